@@ -1,0 +1,367 @@
+#!/usr/bin/env python
+"""H2O 128^3 RHF Fock-applies/s and force time, mixed precision vs plain FP64.
+
+Workload (one step = one block Fock apply): water with HGH pseudopotentials
+(O Z_ion=6, H Z_ion=1) at R_OH = 1.81 bohr, 104.5 deg plus seeded +-0.05 bohr
+jitter, on a 128^3 grid with h = 0.25 bohr and the 13-point Laplacian; four
+seeded orthonormal occupied orbitals; F phi_i for all four orbitals with the
+10 pair Poisson solves J[phi_i phi_j] on the 256^3 doubled grid. `value` is
+the mixed path (FP32 fields/stencil/FFT/exchange, FP64 and float-float
+reductions) with inputs resident in HBM; `e2e` is the same through the public
+API with the orbitals copied in from pinned host memory and the result copied
+back every step. Also reported: the plain FP64 rate, matvec (one vector,
+4 pair solves) rates, |Delta E| of the energy terms mixed vs FP64, the force
+time of both paths, the roofline of the dominant kernel and of the stencil,
+and the CPU baseline (the NumPy restatement of the reference on the host).
+
+Launch: python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+(N > 1 via torch.distributed.run: independent replicas, one per GPU).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT, H_DEFAULT, N_OCC = 128, 0.25, 4
+METRIC = "H2O 128^3 RHF block Fock-applies/s (mixed FP32/FP64 at |dE|<1uHa) and force time"
+UNIT = "Fock-applies/s"
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def synthetic_water(N: int, h: float, seed: int = 2024):
+    """Seeded geometry and four orthonormal smooth orbitals (float64, host numpy)."""
+    import numpy as np
+    L = N * h
+    rng = np.random.default_rng(seed)
+    half = math.radians(104.5) / 2
+    pos = np.array([[0.0, 0.0, 0.0], [1.81 * math.sin(half), 0.0, 1.81 * math.cos(half)],
+                    [-1.81 * math.sin(half), 0.0, 1.81 * math.cos(half)]])
+    pos = pos + rng.uniform(-0.05, 0.05, (3, 3))
+    a = -L / 2 + (np.arange(N) + 0.5) * h
+    X, Y, Z = np.meshgrid(a, a, a, indexing="ij")
+    orbs = np.empty((N_OCC, N, N, N))
+    for k in range(N_OCC):
+        c = pos[k % 3] + rng.uniform(-0.3, 0.3, 3)
+        al = rng.uniform(0.4, 0.9)
+        w = rng.uniform(-0.3, 0.3, 3)
+        orbs[k] = np.exp(-al * ((X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2)) * (
+            1.0 + w[0] * X + w[1] * Y + w[2] * Z)
+    dV = h ** 3
+    for i in range(N_OCC):
+        for j in range(i):
+            orbs[i] -= np.sum(orbs[i] * orbs[j]) * dV * orbs[j]
+        orbs[i] /= math.sqrt(np.sum(orbs[i] ** 2) * dV)
+    return pos, orbs
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu, self.proc, self.path = gpu, None, f"/tmp/gato_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.remove(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_block_apply_rate(pos, orbs, N, h):
+    """The NumPy restatement of the reference (oracle) on the host cores."""
+    import numpy as np
+    from oracle import gato_np as o
+    g = o.Grid3D(N, N * h)
+    nuc = o.Nuclei(pos, np.array([8.0, 1.0, 1.0]))
+    el = o.water_hgh_elements()
+    V = o.hgh_local_potential(nuc, el, g) + o.hartree_potential(o._density(np.moveaxis(orbs, 0, -1)), g)
+    nl = lambda p: o.hgh_nonlocal_apply(p, nuc, el, g)  # noqa: E731
+    o.fock_apply_block(orbs[:1], V, g, order=4, nl=nl)   # warm the kernel-spectrum cache
+    t0 = time.perf_counter()
+    o.fock_apply_block(orbs, V, g, order=4, nl=nl)
+    dt = time.perf_counter() - t0
+    return 1.0 / dt, dt
+
+
+def run_reference(args):
+    """`--impl reference`: the reference algorithm's CPU implementation (the
+    oracle port; the JAX reference is not installable offline), same metric."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+    from oracle import gato_np as o
+    N, h = args.N, H_DEFAULT
+    pos, orbs = synthetic_water(N, h)
+    g = o.Grid3D(N, N * h)
+    nuc = o.Nuclei(pos, np.array([8.0, 1.0, 1.0]))
+    el = o.water_hgh_elements()
+    V = o.hgh_local_potential(nuc, el, g) + o.hartree_potential(o._density(np.moveaxis(orbs, 0, -1)), g)
+    nl = lambda p: o.hgh_nonlocal_apply(p, nuc, el, g)  # noqa: E731
+    for _ in range(args.warmup):
+        o.fock_apply_block(orbs, V, g, order=4, nl=nl)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.fock_apply_block(orbs, V, g, order=4, nl=nl)
+    dt = time.perf_counter() - t0
+    value = args.steps / dt
+    cores = os.cpu_count()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded water geometry and orbitals)",
+            "config": {"workload": f"H2O HGH {N}^3 h={h} block Fock apply, 4 orbitals, 10 pair Poisson solves"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} block Fock applies of the {N}^3 workload"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gato(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    from gato_gb300 import _lib
+    from gato_gb300.geometry import Nuclei
+    from gato_gb300.grid import Grid3D
+    from gato_gb300.physics.water import bo_grad_positions, water_hgh_elements
+    from gato_gb300.pseudopotentials import hgh_local_potential, nonlocal_for
+    from gato_gb300.scf import Operator, _density_fields, from_fields, pair_fields
+    from gato_gb300.solvers.poisson import get_plan
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    N, h = args.N, H_DEFAULT
+    g = Grid3D(N, N * h)
+    dev = torch.device("cuda", local)
+    pos, orbs = synthetic_water(N, h)
+    nuc = Nuclei(torch.tensor(pos), torch.tensor([8.0, 1.0, 1.0], dtype=torch.float64))
+    el = water_hgh_elements()
+    n3 = N ** 3
+    eps = h / 2
+
+    def build(dtype):
+        fields = torch.tensor(orbs, device=dev).to(dtype).contiguous()
+        V_loc = hgh_local_potential(nuc, el, g, dtype)
+        nl = nonlocal_for(nuc, el, g, dtype)
+        plan = get_plan(N, h, eps, dtype, pair_fields(N_OCC))
+        V_tot = (V_loc + plan.potential(_density_fields(fields))).contiguous()
+        op = Operator(g, dtype, 4, "dirichlet")
+        op.set_potential(V_tot)
+        op.set_nonlocal(nl)
+        op.set_exchange(plan, fields)
+        return dict(fields=fields, V_loc=V_loc, nl=nl, plan=plan, op=op, out=torch.empty_like(fields))
+
+    s32, s64 = build(torch.float32), build(torch.float64)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        evs = []
+        for _ in range(steps):
+            flush.fill_(1.0)                     # L2 flush, outside the timed events
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) * 1e-3 for a, b in evs]
+
+    # ---- headline: mixed block Fock apply, inputs resident ----------------------
+    op32 = s32["op"]
+    for _ in range(args.warmup):
+        op32.apply_block(s32["out"])
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = _lib.launch_count()
+    with ClockSampler(local) as clk:
+        times = timed(lambda: op32.apply_block(s32["out"]), args.steps, 0)
+    launches = (_lib.launch_count() - l0) // max(args.steps, 1) * args.steps
+    t_local = sum(times)
+    t_max = t_local
+    if world > 1:
+        tt = torch.tensor([t_local], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt)
+    value = world * args.steps / t_max
+
+    # ---- plain FP64 and matvec rates ----------------------------------------------
+    k64 = max(2, args.steps // 4)
+    t64 = timed(lambda: s64["op"].apply_block(s64["out"]), k64, 1)
+    rate64 = k64 / sum(t64)
+    psi32, psi64 = s32["fields"][1].clone(), s64["fields"][1].clone()
+    o32, o64 = torch.empty_like(psi32), torch.empty_like(psi64)
+    tm32 = timed(lambda: op32.apply(psi32, o32), args.steps, 2)
+    tm64 = timed(lambda: s64["op"].apply(psi64, o64), k64, 1)
+
+    # ---- accuracy: energy terms of the same orbitals, mixed vs FP64 ---------------
+    e32 = s32["op"].energy_terms(s32["V_loc"]).cpu().numpy()
+    e64 = s64["op"].energy_terms(s64["V_loc"]).cpu().numpy()
+    dE = float(abs(e32.sum() - e64.sum()))
+
+    # ---- force time ---------------------------------------------------------------
+    def force_ms(st):
+        o = from_fields(st["fields"])
+        bo_grad_positions(nuc.positions, nuc.charges, o, el, g)   # warm
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        f = bo_grad_positions(nuc.positions, nuc.charges, o, el, g)
+        torch.cuda.synchronize()
+        return 1e3 * (time.perf_counter() - t0), f
+    f32_ms, F32 = force_ms(s32)
+    f64_ms, F64 = force_ms(s64)
+    dF = float(torch.max(torch.abs(F32 - F64)))
+
+    # ---- roofline: dominant kernel (x-pass: FFT, kernel multiply, inverse FFT) ----
+    peak, peak_kind = measured_peaks()
+    M, Hh = 2 * N, N + 1
+    nf = (N_OCC * (N_OCC + 1) // 2 + 1) // 2
+    plan = s32["plan"]
+    tx = timed(lambda: _lib.call("gato_poisson_stage", plan.handle, 2, nf, torch.cuda.current_stream().cuda_stream),
+               max(3, args.steps), 2)
+    tx_avg = sum(tx) / len(tx)
+    bytes_x = nf * (2 * N * M * M * 8) + Hh ** 3 * 4
+    # stencil: 3 N^3 s per field (psi, V, out), four fields per launch
+    from gato_gb300.operators import stencil
+    st_in, st_out = s32["fields"], torch.empty_like(s32["fields"])
+    V32 = s32["op"]._keep["V"]
+    ts = timed(lambda: stencil(st_in, h, "dirichlet", 4, -0.5 / h ** 2, V=V32, out=st_out), max(3, args.steps), 2)
+    ts_avg = sum(ts) / len(ts)
+    bytes_s = 3 * n3 * 4 * N_OCC
+
+    # ---- e2e: public API with host buffers ---------------------------------------
+    host_in = torch.tensor(orbs, dtype=torch.float32).pin_memory()
+    host_out = torch.empty_like(host_in).pin_memory()
+
+    def e2e_step():
+        s32["fields"].copy_(host_in, non_blocking=True)
+        op32.apply_block(s32["out"])
+        host_out.copy_(s32["out"], non_blocking=True)
+    te = timed(e2e_step, args.steps, 2)
+    e2e_val = world * args.steps / sum(te)
+
+    if rank != 0:
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+    cpu = None
+    if not args.no_cpu:
+        rate, dt = cpu_block_apply_rate(pos, orbs, N, h)
+        cpu = {"value": rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"1 block Fock apply of the {N}^3 workload ({dt:.2f} s) with scipy.fft on all cores"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded water geometry and orbitals)",
+        "config": {"workload": f"H2O HGH {N}^3 h={h} block Fock apply: 4 orbitals, 10 pair Poisson solves "
+                               f"on the {2 * N}^3 doubled grid", "precision": "mixed", "N": N, "h": h,
+                   "n_occ": N_OCC, "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas"},
+        "clocks": clk.summary(),
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": host_in.numel() * 4,
+                "d2h_bytes_per_step": host_out.numel() * 4},
+        "gpu_launches": int(launches),
+        "roofline": {"kernel": "k_cols<float2, FMI> (x FFT, kernel multiply, inverse x FFT)", "bound": "hbm",
+                     "achieved": bytes_x / tx_avg / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": bytes_x / tx_avg / 1e9 / peak, "traffic": None, "peak_kind": peak_kind,
+                     "algorithmic_bytes": bytes_x, "avg_launch_us": tx_avg * 1e6},
+        "roofline_stencil": {"bound": "hbm", "achieved": bytes_s / ts_avg / 1e9, "peak": peak, "unit": "GB/s",
+                             "frac": bytes_s / ts_avg / 1e9 / peak, "avg_launch_us": ts_avg * 1e6},
+        "cpu_baseline": cpu,
+        "fp64_block_applies_per_s": rate64,
+        "speedup_mixed_vs_fp64": value / world / rate64,
+        "matvec_applies_per_s": {"mixed": args.steps / sum(tm32), "fp64": k64 / sum(tm64)},
+        "energy_terms": {"mixed": e32.tolist(), "fp64": e64.tolist(), "abs_dE_Ha": dE},
+        "force_ms": {"mixed": f32_ms, "fp64": f64_ms, "max_abs_dF_Ha_per_bohr": dF},
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gato", choices=["gato", "reference"])
+    ap.add_argument("--N", type=int, default=N_DEFAULT)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gato(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,139 @@
+// Register-resident two-pass FFT engine for line lengths M = R1 * R2.
+//
+// A CTA transforms L lines at once; each thread owns one line of one stage
+// and keeps its R1 or R2 points in registers. With n = R2 n1 + n2 and
+// k = k1 + R1 k2 the DFT factors as (the "four-step" decomposition)
+//   X[k1 + R1 k2] = sum_n2 W_R2^{n2 k2} W_M^{n2 k1} sum_n1 W_R1^{n1 k1} x[R2 n1 + n2]
+// stage 1: thread (line, n2) does the R1-point DFT over n1 (stride R2);
+// stage 2: thread (line, k1) applies W_M^{n2 k1} and the R2-point DFT over
+// n2, leaving X[k1 + R1 k2] in its registers. The inverse runs the same
+// factorisation backwards from that register layout, so a forward transform,
+// a pointwise multiply and an inverse transform cost two shared-memory round
+// trips in total. The in-register DFTs are unrolled with compile-time
+// twiddles (twiddles.cuh). The first N = M/2 inputs are the only nonzero
+// ones in the zero-padded forward transforms (R1 is even, so they are
+// n1 < R1/2), and the inverse keeps only the first M/2 outputs.
+#pragma once
+#include "fft.cuh"
+#include "twiddles.cuh"
+
+namespace gato {
+namespace fft2 {
+
+template <int R> struct Split;
+template <> struct Split<6> { static constexpr int A = 2, B = 3; };
+template <> struct Split<10> { static constexpr int A = 2, B = 5; };
+template <> struct Split<12> { static constexpr int A = 4, B = 3; };
+template <> struct Split<14> { static constexpr int A = 2, B = 7; };
+template <> struct Split<16> { static constexpr int A = 4, B = 4; };
+template <> struct Split<20> { static constexpr int A = 4, B = 5; };
+template <> struct Split<24> { static constexpr int A = 8, B = 3; };
+
+// a * exp(DIR * 2 pi i e / R), e a compile-time constant after unrolling
+template <typename T2, int R, int DIR>
+__device__ __forceinline__ T2 ctw(T2 a, int e) {
+  using Rt = typename CT<T2>::R;
+  if (e == 0) return a;
+  const Rt c = (Rt)TwC<R>::c(e);
+  const Rt s = (Rt)DIR * (Rt)TwC<R>::s(e);
+  T2 r;
+  r.x = a.x * c - a.y * s;
+  r.y = a.x * s + a.y * c;
+  return r;
+}
+
+// In-place R-point DFT in natural order; DIR = -1 forward, +1 inverse (unscaled).
+template <typename T2, int R, int DIR>
+__device__ __forceinline__ void rdft(T2* v) {
+  if constexpr (R == 1) {
+  } else if constexpr (R == 2) {
+    dft2(v);
+  } else if constexpr (R == 4) {
+    dft4(v[0], v[1], v[2], v[3], DIR);
+  } else if constexpr (R == 8) {
+    dft8(v, DIR);
+  } else if constexpr (R == 3 || R == 5 || R == 7) {
+    dft_odd<T2, R>(v, DIR);
+  } else {
+    constexpr int A = Split<R>::A, B = Split<R>::B;
+    T2 y[R];
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) {
+      T2 u[A];
+#pragma unroll
+      for (int n1 = 0; n1 < A; ++n1) u[n1] = v[B * n1 + n2];
+      rdft<T2, A, DIR>(u);
+#pragma unroll
+      for (int k1 = 0; k1 < A; ++k1) y[n2 * A + k1] = ctw<T2, R, DIR>(u[k1], (n2 * k1) % R);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) {
+      T2 u[B];
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) u[n2] = y[n2 * A + k1];
+      rdft<T2, B, DIR>(u);
+#pragma unroll
+      for (int k2 = 0; k2 < B; ++k2) v[k1 + A * k2] = u[k2];
+    }
+  }
+}
+
+template <int R1, int R2> struct Shape {
+  static constexpr int M = R1 * R2;
+  static constexpr int RMAX = R1 > R2 ? R1 : R2;
+};
+
+// Runtime twiddle W_M^{DIR * e} from the shared table tw[e] = exp(-2 pi i e / M).
+template <typename T2, int DIR>
+__device__ __forceinline__ T2 rtw(T2 a, const T2* tw, int e) {
+  T2 w = tw[e];
+  if (DIR > 0) w.y = -w.y;
+  return cmul(a, w);
+}
+
+// Stage 1 of the forward transform for the item (line, n2): reads x[R2 n1 + n2]
+// through `get` (only n1 < R1/2 when HALF), writes Y[n2][k1] to buf.
+template <typename T2, int R1, int R2, bool HALF, typename Get>
+__device__ __forceinline__ void fwd_stage1(T2* buf, int LP, int line, int n2, Get get) {
+  T2 v[R1];
+#pragma unroll
+  for (int n1 = 0; n1 < R1; ++n1) {
+    if (!HALF || n1 < R1 / 2) v[n1] = get(R2 * n1 + n2);
+    else v[n1].x = v[n1].y = 0;
+  }
+  rdft<T2, R1, -1>(v);
+#pragma unroll
+  for (int k1 = 0; k1 < R1; ++k1) buf[(n2 * R1 + k1) * LP + line] = v[k1];
+}
+
+// Stage 2 of the forward transform for (line, k1): X[k2] = spectrum at k1 + R1 k2.
+template <typename T2, int R1, int R2>
+__device__ __forceinline__ void fwd_stage2(const T2* buf, int LP, int line, int k1, const T2* tw,
+                                           T2* X) {
+#pragma unroll
+  for (int n2 = 0; n2 < R2; ++n2) X[n2] = rtw<T2, -1>(buf[(n2 * R1 + k1) * LP + line], tw, n2 * k1);
+  rdft<T2, R2, -1>(X);
+}
+
+// Inverse stage A for (line, k1) holding X[k2] = spectrum at k1 + R1 k2: writes Z to buf.
+template <typename T2, int R1, int R2>
+__device__ __forceinline__ void inv_stageA(T2* buf, int LP, int line, int k1, const T2* tw, T2* X) {
+  rdft<T2, R2, +1>(X);
+#pragma unroll
+  for (int n2 = 0; n2 < R2; ++n2) buf[(n2 * R1 + k1) * LP + line] = rtw<T2, +1>(X[n2], tw, n2 * k1);
+}
+
+// Inverse stage B for (line, n2): outputs x[n2 + R2 n1] through `put` (n1 < R1/2 when HALF).
+template <typename T2, int R1, int R2, bool HALF, typename Put>
+__device__ __forceinline__ void inv_stageB(const T2* buf, int LP, int line, int n2, Put put) {
+  T2 w[R1];
+#pragma unroll
+  for (int k1 = 0; k1 < R1; ++k1) w[k1] = buf[(n2 * R1 + k1) * LP + line];
+  rdft<T2, R1, +1>(w);
+#pragma unroll
+  for (int n1 = 0; n1 < R1; ++n1)
+    if (!HALF || n1 < R1 / 2) put(n2 + R2 * n1, w[n1]);
+}
+
+}  // namespace fft2
+}  // namespace gato

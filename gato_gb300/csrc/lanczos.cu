@@ -1,0 +1,517 @@
+// Lanczos with full reorthogonalisation (solvers/lanczos.py:110-206).
+//
+// The m-step loop runs on the device with no host synchronisation: every
+// scalar (alpha_j, beta_j, Gram-Schmidt coefficients) lives in device memory
+// and is read by the next kernel. Per step:
+//   F v_j -> W (the operator writes straight into the Krylov slot j+1)
+//   alpha  : alpha_j = dV <v_j, W - beta_{j-1} v_{j-1}>
+//   gemv_t : c_k = dV <v_k, w''>, w'' = W - beta_{j-1} v_{j-1} - alpha_j v_j, k <= j
+//   gemv_n : W <- w'' - sum_k c_k v_k, with |W|^2 partials
+//   [further classical Gram-Schmidt passes when reorth_passes > 1]
+//   scale  : beta_j = sqrt(dV |W|^2), v_{j+1} = W / beta_j (zero if beta_j = 0)
+// This is the reference's three-term step followed by a Gram-Schmidt sweep
+// against v_0..v_j; the classical sweep reads the basis twice per step in
+// two launches where modified Gram-Schmidt needs one dependent pass per
+// vector, and (with the three-term part removed first) it keeps the basis
+// orthogonal to working precision.
+//
+// The m x m tridiagonal eigenproblem is solved on the device in FP64:
+// eigenvalue k by multisection on the Sturm count (32 lanes bisect at once),
+// eigenvectors by inverse iteration with the partial-pivoting tridiagonal LU
+// (the LAPACK dgttrf/dgtts2 scheme), re-orthogonalised within clusters of
+// close eigenvalues. Ritz vectors are sum_j Y[j,k] v_j.
+#include <cmath>
+
+#include "op.cuh"
+
+namespace gato {
+int dot_impl(int dtype, const void* a, const void* b, int64_t n, double scale, double* out,
+             cudaStream_t s);
+}
+
+namespace gato {
+
+namespace {
+
+constexpr int kLzThreads = 256;
+constexpr int kEPT = 8;                         // elements per thread per chunk
+constexpr int kChunk = kLzThreads * kEPT;       // elements per block-chunk
+
+// Up to two vectors subtracted from W on the fly: w = W - s0 u0 - s1 u1, the
+// scalars read from device memory (beta_{j-1} and alpha_j of the step).
+template <typename T>
+struct Pre {
+  const T* u[2] = {nullptr, nullptr};
+  const double* s[2] = {nullptr, nullptr};
+};
+
+template <typename T>
+__device__ __forceinline__ void pre_scalars(const Pre<T>& p, T* sc) {
+  sc[0] = p.u[0] ? (T)p.s[0][0] : (T)0;
+  sc[1] = p.u[1] ? (T)p.s[1][0] : (T)0;
+}
+
+template <typename T>
+__device__ __forceinline__ T pre_load(const T* W, const Pre<T>& p, const T* sc, int64_t i) {
+  T w = W[i];
+  if (p.u[0]) w -= sc[0] * p.u[0][i];
+  if (p.u[1]) w -= sc[1] * p.u[1][i];
+  return w;
+}
+
+// c_k partials: part[k * nblk + block] = sum_i V_k[i] w[i]
+template <typename T>
+__global__ void __launch_bounds__(kLzThreads)
+    k_gemv_t(const T* __restrict__ V, int64_t ld, int nk, const T* __restrict__ W, Pre<T> pre,
+             int64_t n, double* part) {
+  extern __shared__ double wacc[];   // [warp][k]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = kLzThreads / 32;
+  T sc[2];
+  pre_scalars(pre, sc);
+  for (int i = threadIdx.x; i < nw * nk; i += blockDim.x) wacc[i] = 0.0;
+  __syncthreads();
+  for (int64_t base = (int64_t)blockIdx.x * kChunk; base < n; base += (int64_t)gridDim.x * kChunk) {
+    T w[kEPT];
+#pragma unroll
+    for (int e = 0; e < kEPT; ++e) {
+      const int64_t i = base + e * kLzThreads + threadIdx.x;
+      w[e] = i < n ? pre_load(W, pre, sc, i) : (T)0;
+    }
+    for (int k = 0; k < nk; ++k) {
+      const T* vk = V + (int64_t)k * ld;
+      T s = (T)0;
+#pragma unroll
+      for (int e = 0; e < kEPT; ++e) {
+        const int64_t i = base + e * kLzThreads + threadIdx.x;
+        if (i < n) s = fma(vk[i], w[e], s);
+      }
+      double d;
+      if constexpr (sizeof(T) == 4) d = (double)warp_sumf(s);
+      else d = warp_sum(s);
+      if (lane == 0) wacc[warp * nk + k] += d;
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s += wacc[w * nk + k];
+    part[(int64_t)k * gridDim.x + blockIdx.x] = s;
+  }
+}
+
+// W <- W - pre - sum_k c_k v_k ; norm partials part[block]
+template <typename T>
+__global__ void __launch_bounds__(kLzThreads)
+    k_gemv_n(const T* __restrict__ V, int64_t ld, int nk, T* __restrict__ W, Pre<T> pre,
+             const double* __restrict__ c, int64_t n, double* part) {
+  extern __shared__ double cs[];
+  __shared__ double sh[32];
+  for (int k = threadIdx.x; k < nk; k += blockDim.x) cs[k] = c[k];
+  __syncthreads();
+  T sc[2];
+  pre_scalars(pre, sc);
+  Acc<T> acc;
+  for (int64_t base = (int64_t)blockIdx.x * kChunk; base < n; base += (int64_t)gridDim.x * kChunk) {
+    T w[kEPT];
+#pragma unroll
+    for (int e = 0; e < kEPT; ++e) {
+      const int64_t i = base + e * kLzThreads + threadIdx.x;
+      w[e] = i < n ? pre_load(W, pre, sc, i) : (T)0;
+    }
+    for (int k = 0; k < nk; ++k) {
+      const T* vk = V + (int64_t)k * ld;
+      const T ck = (T)cs[k];
+#pragma unroll
+      for (int e = 0; e < kEPT; ++e) {
+        const int64_t i = base + e * kLzThreads + threadIdx.x;
+        if (i < n) w[e] -= ck * vk[i];
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < kEPT; ++e) {
+      const int64_t i = base + e * kLzThreads + threadIdx.x;
+      if (i < n) {
+        W[i] = w[e];
+        acc.add_prod(w[e], w[e]);
+      }
+    }
+  }
+  const double s = block_sum(acc.value(), sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// beta = sqrt(nrm); v = W / beta (or 0); betas_out[0] = beta
+template <typename T>
+__global__ void k_beta_scale(T* W, int64_t n, const double* nrm, double* beta_out) {
+  const double beta = sqrt(nrm[0]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) beta_out[0] = beta;
+  const double inv = beta > 0 ? 1.0 / beta : 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    W[i] = beta > 0 ? (T)((double)W[i] * inv) : (T)0;
+}
+
+template <typename T>
+__global__ void k_scale_copy(const T* __restrict__ src, T* dst, int64_t n, const double* nrm) {
+  const double inv = 1.0 / sqrt(nrm[0]);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (T)((double)src[i] * inv);
+}
+
+__global__ void k_copy_double(const double* src, double* dst) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) dst[0] = src[0];
+}
+
+// ---- tridiagonal eigensolver (FP64, one block) ----------------------------------
+
+// number of eigenvalues of T strictly below x (Sturm count via LDL^T pivots)
+__device__ int sturm_count(const double* a, const double* e2, int m, double x, double pivmin) {
+  int cnt = 0;
+  double q = a[0] - x;
+  if (fabs(q) < pivmin) q = -pivmin;
+  if (q < 0) ++cnt;
+  for (int i = 1; i < m; ++i) {
+    q = (a[i] - x) - e2[i - 1] / q;
+    if (fabs(q) < pivmin) q = -pivmin;
+    if (q < 0) ++cnt;
+  }
+  return cnt;
+}
+
+// Shared: a[m], e[m], e2[m]; eigenvalues -> lam[K]; eigenvectors -> Y[m*K] (column k at Y + k*m)
+// work: global scratch of 5*m*K doubles for the LU factors.
+__global__ void __launch_bounds__(256) k_tridiag_eig(const double* alpha, const double* beta, int m, int K, double* evals,
+                              double* Y, double* work, int* flag, double tol, int* err) {
+  extern __shared__ double sm[];
+  double* a = sm;
+  double* e = a + m;
+  double* e2 = e + m;
+  double* lam = e2 + m;         // K
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  for (int i = tid; i < m; i += blockDim.x) {
+    a[i] = alpha[i];
+    e[i] = i < m - 1 ? beta[i] : 0.0;
+    e2[i] = e[i] * e[i];
+  }
+  __syncthreads();
+  // converged flag: any beta_j < tol for j < max(m-1, 1) (lanczos.py:199)
+  if (tid == 0) {
+    int f = 0;
+    const int lim = m - 1 > 1 ? m - 1 : 1;
+    for (int j = 0; j < lim; ++j) f |= beta[j] < tol;
+    flag[0] = f;
+  }
+  // Gershgorin interval
+  __shared__ double glo, ghi, tnorm;
+  if (tid == 0) {
+    double lo = 1e300, hi = -1e300, nm = 0;
+    for (int i = 0; i < m; ++i) {
+      const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < m - 1 ? fabs(e[i]) : 0.0);
+      lo = fmin(lo, a[i] - r);
+      hi = fmax(hi, a[i] + r);
+      nm = fmax(nm, fabs(a[i]) + r);
+    }
+    const double pad = 2.2e-16 * nm * 4 + 1e-300;
+    glo = lo - pad;
+    ghi = hi + pad;
+    tnorm = nm > 0 ? nm : 1.0;
+  }
+  __syncthreads();
+  const double pivmin = 1e-290 > 2.2e-16 * 2.2e-16 * tnorm ? 1e-290 : 1e-300;
+  // multisection: warp w finds eigenvalues k = w, w + nw, ...
+  for (int k = warp; k < K; k += nw) {
+    double lo = glo, hi = ghi;
+    for (int it = 0; it < 80; ++it) {
+      const double width = hi - lo;
+      if (width <= 2.2e-16 * 2 * fmax(fabs(lo), fabs(hi)) + pivmin) break;
+      const double x = lo + width * (double)(lane + 1) / 33.0;
+      const int c = sturm_count(a, e2, m, x, pivmin);
+      // bracket: eigenvalue k lies in [x_i, x_{i+1}) where count(x_i) <= k < count(x_{i+1})
+      const unsigned below = __ballot_sync(0xffffffffu, c <= k);   // lanes whose x is <= lambda_k
+      const int nb = __popc(below);  // counts are monotone: lanes 0..nb-1 have c <= k
+      const double nlo = nb > 0 ? lo + width * (double)nb / 33.0 : lo;
+      const double nhi = nb < 32 ? lo + width * (double)(nb + 1) / 33.0 : hi;
+      lo = nlo;
+      hi = nhi;
+    }
+    if (lane == 0) lam[k] = 0.5 * (lo + hi);
+  }
+  __syncthreads();
+  // inverse iteration: thread k computes eigenvector k
+  for (int k = tid; k < K; k += blockDim.x) {
+    double* dl = work + (int64_t)k * 5 * m;
+    double* d = dl + m;
+    double* du = d + m;
+    double* du2 = du + m;
+    double* x = du2 + m;
+    // start vector
+    for (int i = 0; i < m; ++i) x[i] = 1.0 + 0.25 * sin(0.7 * (i + 1) * (k + 1) + 0.3);
+    const double shift = lam[k];
+    const double tiny = 2.2e-16 * tnorm;
+    for (int iter = 0; iter < 4; ++iter) {
+      // factor (T - shift I) with partial pivoting while eliminating the
+      // right-hand side in the same sweep (refactored every iteration: O(m))
+      for (int i = 0; i < m; ++i) {
+        d[i] = a[i] - shift;
+        dl[i] = e[i];
+        du[i] = e[i];
+        du2[i] = 0.0;
+      }
+      // forward elimination applied simultaneously to x (right-hand side)
+      for (int i = 0; i < m - 1; ++i) {
+        if (fabs(d[i]) >= fabs(dl[i])) {
+          if (d[i] == 0.0) d[i] = tiny;
+          const double f = dl[i] / d[i];
+          d[i + 1] -= f * du[i];
+          x[i + 1] -= f * x[i];
+          du2[i] = 0.0;
+        } else {
+          // interchange rows i and i+1
+          const double f = d[i] / dl[i];
+          d[i] = dl[i];
+          const double t = du[i];
+          du[i] = d[i + 1];
+          d[i + 1] = t - f * d[i + 1];
+          if (i < m - 2) {
+            du2[i] = du[i + 1];
+            du[i + 1] = -f * du[i + 1];
+          }
+          const double xt = x[i];
+          x[i] = x[i + 1];
+          x[i + 1] = xt - f * x[i + 1];
+        }
+      }
+      if (d[m - 1] == 0.0) d[m - 1] = tiny;
+      // back substitution
+      x[m - 1] /= d[m - 1];
+      if (m > 1) x[m - 2] = (x[m - 2] - du[m - 2] * x[m - 1]) / d[m - 2];
+      for (int i = m - 3; i >= 0; --i) x[i] = (x[i] - du[i] * x[i + 1] - du2[i] * x[i + 2]) / d[i];
+      double nrm = 0.0;
+      for (int i = 0; i < m; ++i) nrm += x[i] * x[i];
+      nrm = sqrt(nrm);
+      if (!(nrm > 0) || !isfinite(nrm)) {
+        if (err) atomicExch(err, 201);
+        nrm = 1.0;
+      }
+      for (int i = 0; i < m; ++i) x[i] /= nrm;
+    }
+  }
+  __syncthreads();
+  // cluster re-orthogonalisation (thread 0), then sign: largest component positive
+  if (tid == 0) {
+    const double close = 1e-7 * tnorm;
+    for (int k = 0; k < K; ++k) {
+      double* xk = work + (int64_t)k * 5 * m + 4 * m;
+      for (int l = 0; l < k; ++l) {
+        if (fabs(lam[k] - lam[l]) > close) continue;
+        const double* xl = work + (int64_t)l * 5 * m + 4 * m;
+        double dot = 0;
+        for (int i = 0; i < m; ++i) dot += xl[i] * xk[i];
+        for (int i = 0; i < m; ++i) xk[i] -= dot * xl[i];
+        double nrm = 0;
+        for (int i = 0; i < m; ++i) nrm += xk[i] * xk[i];
+        nrm = sqrt(nrm);
+        for (int i = 0; i < m; ++i) xk[i] /= nrm;
+      }
+      int imax = 0;
+      for (int i = 1; i < m; ++i)
+        if (fabs(xk[i]) > fabs(xk[imax])) imax = i;
+      const double sg = xk[imax] < 0 ? -1.0 : 1.0;
+      for (int i = 0; i < m; ++i) Y[(int64_t)k * m + i] = sg * xk[i];
+      evals[k] = lam[k];
+    }
+  }
+}
+
+// out[k] = sum_j Y[k*m + j] v_j for k in [k0, k0 + KB)
+template <typename T, int KB>
+__global__ void __launch_bounds__(256) k_ritz(const T* __restrict__ V, int64_t ld, int m,
+                                              const double* __restrict__ Y, int k0, int K,
+                                              T* __restrict__ out, int64_t n) {
+  extern __shared__ double ys[];   // [KB][m]
+  const int kb = min(KB, K - k0);
+  for (int i = threadIdx.x; i < kb * m; i += blockDim.x) ys[i] = Y[(int64_t)(k0 + i / m) * m + i % m];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    T acc[KB];
+#pragma unroll
+    for (int k = 0; k < KB; ++k) acc[k] = (T)0;
+    for (int j = 0; j < m; ++j) {
+      const T v = V[(int64_t)j * ld + i];
+#pragma unroll
+      for (int k = 0; k < KB; ++k)
+        if (k < kb) acc[k] = fma((T)ys[k * m + j], v, acc[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < KB; ++k)
+      if (k < kb) out[(int64_t)(k0 + k) * n + i] = acc[k];
+  }
+}
+
+struct LzScratch {
+  double *part, *coef, *nrm, *Y, *work;
+  int nblk;
+};
+
+inline int lz_nblk(int64_t n) { return (int)std::min<int64_t>((n + kChunk - 1) / kChunk, 2 * 152 * 2); }
+
+int lz_scratch(cudaStream_t s, int64_t n, int m, int K, LzScratch& z) {
+  z.nblk = lz_nblk(n);
+  // partials (m+1)*nblk, coefficients (m+1), norm, Y (m*K), LU work 5*m*K
+  const size_t need = ((size_t)(m + 1) * z.nblk + (m + 1) + 8 + (size_t)m * K + (size_t)5 * m * K) *
+                      sizeof(double);
+  z.part = (double*)stream_scratch(s, need, kSlotLanczos);
+  if (!z.part) return fail(GATO_ENOMEM, "lanczos: scratch allocation failed");
+  z.coef = z.part + (size_t)(m + 1) * z.nblk;
+  z.nrm = z.coef + (m + 1);
+  z.Y = z.nrm + 8;
+  z.work = z.Y + (size_t)m * K;
+  return GATO_OK;
+}
+
+// v0 = psi0 / sqrt(<psi0, psi0> dV)
+template <typename T>
+int lz_begin(const void* psi0, T* Vb, int64_t n, double dV, const LzScratch& z, cudaStream_t s) {
+  GATO_TRY(dot_impl(sizeof(T) == 8 ? GATO_F64 : GATO_F32, psi0, psi0, n, dV, z.nrm, s));
+  k_scale_copy<T><<<grid_for(n, 256), 256, 0, s>>>((const T*)psi0, Vb, n, z.nrm);
+  GATO_LAUNCH_TRY();
+  return GATO_OK;
+}
+
+// Slot j+1 holds F v_j on entry and v_{j+1} on exit. The three-term part
+// comes first, as in the reference: w' = F v_j - beta_{j-1} v_{j-1},
+// alpha_j = <v_j, w'>, w'' = w' - alpha_j v_j; then classical Gram-Schmidt
+// of w'' against v_0..v_j (reorth_passes times). Removing the large alpha_j
+// component before the projection keeps one classical pass as orthogonal as
+// the reference's modified Gram-Schmidt.
+template <typename T>
+int lz_step(T* Vb, int64_t n, double dV, int j, int passes, double* alphas, double* betas,
+            const LzScratch& z, cudaStream_t s) {
+  T* W = Vb + (int64_t)(j + 1) * n;
+  T* vj = Vb + (int64_t)j * n;
+  Pre<T> p1;
+  if (j > 0) {
+    p1.u[0] = Vb + (int64_t)(j - 1) * n;
+    p1.s[0] = betas + (j - 1);
+  }
+  const int nk = j + 1;
+  const size_t smt = (size_t)(kLzThreads / 32) * nk * sizeof(double);
+  const size_t smn = (size_t)nk * sizeof(double);
+  if (smt > 48 * 1024)
+    GATO_CUDA_TRY(cudaFuncSetAttribute(k_gemv_t<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt));
+  // alpha_j = dV <v_j, w'>
+  k_gemv_t<T><<<z.nblk, kLzThreads, (kLzThreads / 32) * sizeof(double), s>>>(vj, n, 1, W, p1, n, z.part);
+  GATO_LAUNCH_TRY();
+  GATO_TRY(finalize_sums(z.part, 1, z.nblk, dV, alphas + j, s));
+  Pre<T> p2 = p1;
+  p2.u[1] = vj;
+  p2.s[1] = alphas + j;
+  for (int p = 0; p < passes; ++p) {
+    const Pre<T>& pp = p == 0 ? p2 : Pre<T>();
+    k_gemv_t<T><<<z.nblk, kLzThreads, smt, s>>>(Vb, n, nk, W, pp, n, z.part);
+    GATO_LAUNCH_TRY();
+    GATO_TRY(finalize_sums(z.part, nk, z.nblk, dV, z.coef, s));
+    k_gemv_n<T><<<z.nblk, kLzThreads, smn, s>>>(Vb, n, nk, W, pp, z.coef, n, z.part);
+    GATO_LAUNCH_TRY();
+  }
+  GATO_TRY(finalize_sums(z.part, 1, z.nblk, dV, z.nrm, s));
+  k_beta_scale<T><<<grid_for(n, 256), 256, 0, s>>>(W, n, z.nrm, betas + j);
+  GATO_LAUNCH_TRY();
+  return GATO_OK;
+}
+
+template <typename T>
+int lz_finish(const T* Vb, int64_t n, int m, int K, double tol, const double* alphas,
+              const double* betas, double* evals, T* evecs, int* flag, const LzScratch& z,
+              cudaStream_t s) {
+  const size_t sme = (size_t)(3 * m + K + 8) * sizeof(double);
+  if (sme > 48 * 1024)
+    GATO_CUDA_TRY(cudaFuncSetAttribute(k_tridiag_eig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sme));
+  k_tridiag_eig<<<1, 256, sme, s>>>(alphas, betas, m, K, evals, z.Y, z.work, flag, tol,
+                                     device_error_word());
+  GATO_LAUNCH_TRY();
+  constexpr int KB = 4;
+  const size_t smr = (size_t)KB * m * sizeof(double);
+  if (smr > 48 * 1024)
+    GATO_CUDA_TRY(cudaFuncSetAttribute(k_ritz<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
+  for (int k0 = 0; k0 < K; k0 += KB) {
+    k_ritz<T, KB><<<grid_for(n, 256, 152 * 8), 256, smr, s>>>(Vb, n, m, z.Y, k0, K, evecs, n);
+    GATO_LAUNCH_TRY();
+  }
+  return GATO_OK;
+}
+
+template <typename T>
+int lanczos_typed(gato_operator& op, const void* psi0, int m, int K, double tol, int passes,
+                  void* krylov, double* evals, void* evecs, double* alphas, double* betas,
+                  int* flag, cudaStream_t s) {
+  const int64_t n = op_n3(op);
+  T* Vb = (T*)krylov;
+  LzScratch z;
+  GATO_TRY(lz_scratch(s, n, m, K, z));
+  GATO_TRY(lz_begin<T>(psi0, Vb, n, op.dV, z, s));
+  for (int j = 0; j < m; ++j) {
+    GATO_TRY(op_apply(op, Vb + (int64_t)j * n, Vb + (int64_t)(j + 1) * n, s));
+    GATO_TRY(lz_step<T>(Vb, n, op.dV, j, passes, alphas, betas, z, s));
+  }
+  return lz_finish<T>(Vb, n, m, K, tol, alphas, betas, evals, (T*)evecs, flag, z, s);
+}
+
+}  // namespace
+
+}  // namespace gato
+
+using namespace gato;
+
+extern "C" int gato_lanczos(gato_op_t op, const void* psi0, int m, int K, double tol,
+                            int reorth_passes, void* krylov, double* evals_dev, void* evecs,
+                            double* alphas_dev, double* betas_dev, int* flag_dev, void* stream) {
+  if (!op || !psi0 || !krylov || !evals_dev || !evecs || !alphas_dev || !betas_dev || !flag_dev)
+    return fail(GATO_EBADARG, "gato_lanczos: NULL argument");
+  if (m < 1 || K < 1 || K > m) return fail(GATO_EBADARG, "gato_lanczos: need 1 <= K <= m (m=%d K=%d)", m, K);
+  if (K > 1024) return fail(GATO_EUNSUPPORTED, "gato_lanczos: at most 1024 eigenpairs");
+  if (reorth_passes < 1 || reorth_passes > 2) return fail(GATO_EBADARG, "reorth_passes must be 1 or 2");
+  cudaStream_t s = as_stream(stream);
+  if (op->dtype == GATO_F64)
+    return lanczos_typed<double>(*op, psi0, m, K, tol, reorth_passes, krylov, evals_dev, evecs,
+                                 alphas_dev, betas_dev, flag_dev, s);
+  return lanczos_typed<float>(*op, psi0, m, K, tol, reorth_passes, krylov, evals_dev, evecs,
+                              alphas_dev, betas_dev, flag_dev, s);
+}
+
+extern "C" int gato_lanczos_begin(int dtype, int64_t n, double dV, const void* psi0, void* krylov,
+                                  int m, int K, void* stream) {
+  if (!psi0 || !krylov || n < 1 || m < 1 || K < 1 || K > m) return fail(GATO_EBADARG, "gato_lanczos_begin: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  LzScratch z;
+  GATO_TRY(lz_scratch(s, n, m, K, z));
+  if (dtype == GATO_F64) return lz_begin<double>(psi0, (double*)krylov, n, dV, z, s);
+  return lz_begin<float>(psi0, (float*)krylov, n, dV, z, s);
+}
+
+extern "C" int gato_lanczos_step(int dtype, int64_t n, double dV, void* krylov, int j, int m, int K,
+                                 int reorth_passes, double* alphas_dev, double* betas_dev,
+                                 void* stream) {
+  if (!krylov || !alphas_dev || !betas_dev || j < 0 || j >= m) return fail(GATO_EBADARG, "gato_lanczos_step: bad arguments");
+  if (reorth_passes < 1 || reorth_passes > 2) return fail(GATO_EBADARG, "reorth_passes must be 1 or 2");
+  cudaStream_t s = as_stream(stream);
+  LzScratch z;
+  GATO_TRY(lz_scratch(s, n, m, K, z));
+  if (dtype == GATO_F64) return lz_step<double>((double*)krylov, n, dV, j, reorth_passes, alphas_dev, betas_dev, z, s);
+  return lz_step<float>((float*)krylov, n, dV, j, reorth_passes, alphas_dev, betas_dev, z, s);
+}
+
+extern "C" int gato_lanczos_finish(int dtype, int64_t n, const void* krylov, int m, int K, double tol,
+                                   const double* alphas_dev, const double* betas_dev,
+                                   double* evals_dev, void* evecs, int* flag_dev, void* stream) {
+  if (!krylov || !alphas_dev || !betas_dev || !evals_dev || !evecs || !flag_dev || m < 1 || K < 1 || K > m)
+    return fail(GATO_EBADARG, "gato_lanczos_finish: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  LzScratch z;
+  GATO_TRY(lz_scratch(s, n, m, K, z));
+  if (dtype == GATO_F64)
+    return lz_finish<double>((const double*)krylov, n, m, K, tol, alphas_dev, betas_dev, evals_dev, (double*)evecs, flag_dev, z, s);
+  return lz_finish<float>((const float*)krylov, n, m, K, tol, alphas_dev, betas_dev, evals_dev, (float*)evecs, flag_dev, z, s);
+}

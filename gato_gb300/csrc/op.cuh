@@ -1,0 +1,25 @@
+// Matrix-free operator F = -1/2 L + V [+ V_nl] [- K] (internal API).
+#pragma once
+#include "common.cuh"
+#include "hgh.cuh"
+#include "poisson.cuh"
+
+struct gato_operator {
+  int dtype = GATO_F64;
+  int N = 0;
+  double h = 0, dV = 0;
+  int order = 4, boundary = GATO_DIRICHLET;
+  const void* V = nullptr;
+  gato_nonlocal* nl = nullptr;
+  gato_poisson_plan* pp = nullptr;
+  const void* orbitals = nullptr;
+  int n_orb = 0;
+  double* dscratch = nullptr;   // small device doubles
+  void* rho = nullptr;          // N^3 density scratch for the energy terms
+};
+
+namespace gato {
+int op_apply(gato_operator& op, const void* in, void* out, cudaStream_t s);
+inline size_t op_esize(const gato_operator& op) { return op.dtype == GATO_F64 ? 8 : 4; }
+inline int64_t op_n3(const gato_operator& op) { return (int64_t)op.N * op.N * op.N; }
+}  // namespace gato

@@ -1,0 +1,99 @@
+// Hockney doubled-grid Poisson plan and batched pair solves (internal API).
+#pragma once
+#include "common.cuh"
+#include "fft.cuh"
+
+namespace gato {
+
+constexpr int kMaxIn = 12;      // input fields a pass can read (orbitals, psi, rho)
+constexpr int kMaxOut = 8;      // output fields a pass can accumulate into
+constexpr int kMaxFields = 40;  // complex fields (= two real densities) per call
+
+// One real density packed into the real or imaginary part of a complex field,
+// and what the epilogue does with its potential J.
+struct PartDesc {
+  int8_t a = -1, b = -1;          // density = in[a] * in[b] (b < 0: in[a]); a < 0: unused
+  int8_t nt = 0;                  // accumulation terms
+  int8_t to[2] = {0, 0};          // out[to] += coef * in[tc] * J   (tc < 0: * 1)
+  int8_t tc[2] = {-1, -1};
+  int8_t eslot = 0;               // energy mode: slot += ew * density * J
+  float coef[2] = {0.f, 0.f};
+  double ew = 0.0;
+};
+struct FieldDesc {
+  PartDesc p[2];
+};
+struct PassArgs {
+  const void* in[kMaxIn] = {};
+  void* out[kMaxOut] = {};
+  int nout = 0;
+  int nf = 0;
+  FieldDesc f[kMaxFields];
+};
+
+struct PoissonPlan {
+  int dtype = GATO_F64;
+  int N = 0, M = 0, H = 0;
+  int max_fields = 0;
+  double h = 0, eps = 0, dV = 0;
+  FftPlanDev fp{};
+  void* ghat = nullptr;    // H^3 octant of the kernel spectrum, x dV / M^3
+  void* tw = nullptr;      // M twiddles exp(-2 pi i k / M)
+  void* S1 = nullptr;      // max_fields x N x N x M complex
+  void* S2 = nullptr;      // max_fields x N x M x M complex
+  double* partials = nullptr;
+  int npart_cap = 0;
+  int group = 0;           // fields per launch group (0: max_fields)
+  int engine = 0;          // 0: register two-pass kernels where M allows, 1: generic Stockham
+};
+
+enum PoissonEpi { EPI_ACC = 0, EPI_ENERGY = 1 };
+
+enum ColMode { COL_FWD = 0, COL_INV = 1, COL_FMI = 2 };
+
+// Geometry of a batched strided-line pass over [field][outer][pos][col].
+struct ColGeom {
+  int64_t in_fs, out_fs;   // field strides (elements)
+  int64_t in_os, out_os;   // outer strides
+  int64_t in_ps, out_ps;   // position strides
+  int ncols;               // contiguous columns (lines)
+  int nin, nout;           // input positions, output positions kept
+};
+
+template <typename T>
+__device__ __forceinline__ T dens(const PartDesc& d, const void* const* in, int64_t gi) {
+  T v = reinterpret_cast<const T*>(in[d.a])[gi];
+  if (d.b >= 0) v *= reinterpret_cast<const T*>(in[d.b])[gi];
+  return v;
+}
+
+// Register-resident two-pass kernels for the common sizes M = 2N (see
+// fft2.cuh); each returns kNotHandled when M has no instantiation.
+namespace fast {
+constexpr int kNotHandled = 1;
+template <typename T> int rows_L(int M);   // lines per CTA of the z kernels, 0 if unsupported
+template <typename T>
+int cols(int M, int mode, const typename Cplx<T>::type* in, typename Cplx<T>::type* out,
+         const ColGeom& g, int outer, int nf, const typename Cplx<T>::type* tw, const T* ghat,
+         int H, cudaStream_t s);
+template <typename T>
+int rows_fwd(int M, const PassArgs& a, int f0, int nfg, typename Cplx<T>::type* S1,
+             const typename Cplx<T>::type* tw, cudaStream_t s);
+template <typename T>
+int rows_inv(int M, const PassArgs& a, int f0, int nfg, const typename Cplx<T>::type* S1,
+             const typename Cplx<T>::type* tw, int accumulate, bool energy, double* partials,
+             int64_t slot_stride, cudaStream_t s);
+}  // namespace fast
+
+// Runs every field of `args` through the pair-solve pipeline in groups of
+// at most plan.max_fields. EPI_ACC: out[o] = (accumulate ? out[o] : 0) +
+// sum of terms. EPI_ENERGY: energy_dev[slot] = dV * sum of weighted terms
+// (two slots).
+int poisson_run(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate,
+                double* energy_dev, cudaStream_t s);
+
+}  // namespace gato
+
+struct gato_poisson_plan {
+  gato::PoissonPlan p;
+};

@@ -1,0 +1,119 @@
+"""CPU checks of the boundary and the host logic (no kernel is launched).
+
+* libgato_cuda builds for sm_103a, loads, and exports every entry point
+  include/gato.h declares;
+* argument validation maps to the reference's exception types before any
+  CUDA call;
+* host-side helpers (Krylov sizing, pair packing, Adam, E_nn gradient).
+"""
+import ctypes as C
+import os
+import re
+
+import pytest
+import torch
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    src = open(os.path.join(ROOT, "include", "gato.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|long long)\s+(gato_\w+)\s*\(", src, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    from gato_gb300 import _lib
+    L = _lib.lib()
+    syms = header_symbols()
+    assert len(syms) >= 35
+    for s in syms:
+        assert hasattr(L, s), f"{s} declared in gato.h but not exported"
+    assert L.gato_version() == 1
+
+
+def test_python_binding_covers_the_header():
+    from gato_gb300 import _lib
+    declared = set(header_symbols())
+    bound = set(_lib._SIGS) | {"gato_launch_count"}
+    assert declared == bound, declared ^ bound
+
+
+def test_validation_maps_to_reference_exceptions():
+    from gato_gb300 import _lib
+    L = _lib.lib()
+    h = C.c_void_p()
+    with pytest.raises(ValueError, match="order"):
+        _lib.check(L.gato_op_create(0, 16, 0.25, 3, 0, C.byref(h)))
+    with pytest.raises(ValueError, match="boundary"):
+        _lib.check(L.gato_op_create(0, 16, 0.25, 4, 7, C.byref(h)))
+    with pytest.raises(ValueError):
+        _lib.check(L.gato_stencil_apply(0, None, None, None, 1, 8, 8, 8, 1.0, 0, 5, None, 1.0, None))
+    with pytest.raises(ValueError):
+        _lib.check(L.gato_lanczos(None, None, 10, 4, 1e-10, 1, None, None, None, None, None, None, None))
+    with pytest.raises(ValueError):
+        _lib.boundary_code("mystery")
+
+
+def test_unsupported_paths_raise_not_implemented():
+    from gato_gb300 import _lib
+    with pytest.raises(NotImplementedError):
+        _lib.check(_lib.GATO_EUNSUPPORTED)
+    with pytest.raises(TimeoutError):
+        _lib.check(_lib.GATO_ETIMEOUT)
+
+
+def test_no_cpu_fallback():
+    """Without a GPU every operation refuses instead of computing on the host."""
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from gato_gb300.grid import Grid3D, norm_sq
+    from gato_gb300.operators import laplacian
+    with pytest.raises(RuntimeError, match="CUDA"):
+        laplacian(torch.ones(8, 8, 8, dtype=torch.float64), 0.1)
+    with pytest.raises(RuntimeError, match="CUDA"):
+        norm_sq(torch.ones(8, 8, 8, dtype=torch.float64), Grid3D(8, 1.0))
+
+
+def test_krylov_dim_and_pair_packing():
+    from gato_gb300.scf import pair_fields, precision_dtype
+    from gato_gb300.solvers.lanczos import default_krylov_dim
+    assert default_krylov_dim(64, 1) == 80 and default_krylov_dim(96, 1) == 120
+    assert default_krylov_dim(128, 4) == 160 and default_krylov_dim(160, 4) == 200
+    assert default_krylov_dim(40, 4) == 120
+    # n(n+1)/2 pairs + the density, two real densities per complex field
+    assert [pair_fields(n) for n in (1, 2, 3, 4, 5)] == [1, 2, 4, 6, 8]
+    assert precision_dtype("mixed") == torch.float32
+    with pytest.raises(ValueError):
+        precision_dtype("fp16")
+
+
+def test_adam_and_geometry_host_logic():
+    from gato_gb300.geometry import Nuclei, bond_angle, bond_length, center_of_mass, recenter
+    from gato_gb300.geometry_opt import Adam
+    from gato_gb300.physics.water import (pp_nuclear_repulsion, pp_nuclear_repulsion_grad,
+                                          water_hgh_elements, water_initial_geometry)
+    opt = Adam(0.02)
+    g = torch.tensor([[0.3, -2.0, 1e-3]], dtype=torch.float64)
+    assert torch.allclose(opt.update(g), -0.02 * g / (g.abs() + 1e-8), rtol=1e-12)
+    nuc = water_initial_geometry(1.81, 104.5)
+    assert float(bond_length(nuc, 0, 1)) == pytest.approx(1.81)
+    assert float(bond_angle(nuc, 1, 0, 2)) == pytest.approx(104.5 * 3.141592653589793 / 180)
+    assert torch.allclose(center_of_mass(recenter(nuc)), torch.zeros(3, dtype=torch.float64), atol=1e-14)
+    el = water_hgh_elements()
+    p = nuc.positions.clone().requires_grad_(True)
+    E = pp_nuclear_repulsion(Nuclei(p, nuc.charges), el)
+    (ga,) = torch.autograd.grad(E, p)
+    assert torch.allclose(ga, pp_nuclear_repulsion_grad(nuc, el), rtol=1e-12)
+
+
+def test_lookup_and_tables():
+    from gato_gb300.pseudopotentials import CHLORINE_HGH, OXYGEN_HGH, lookup, total_valence_charge
+    from oracle import gato_np as o
+    assert lookup("O") is OXYGEN_HGH and lookup("Cl") is CHLORINE_HGH
+    for sym in ("H", "Li", "O", "Cl"):
+        a, b = lookup(sym), o.lookup(sym)
+        assert (a.Z_ion, a.r_loc, a.c) == (b.Z_ion, b.r_loc, b.c)
+        assert [(p.ell, p.r, p.h) for p in a.projectors] == [(p.ell, p.r, p.h) for p in b.projectors]
+    with pytest.raises(KeyError):
+        lookup("Xx")
+    assert total_valence_charge((lookup("O"), lookup("H"), lookup("H"))) == 8.0
