@@ -214,6 +214,12 @@ def run_gato(args):
 
     s32, s64 = build(torch.float32), build(torch.float64)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    from gato_gb300.autotune import tune_plan
+    tuned = {}
+    for name, st in (("mixed", s32), ("fp64", s64)):
+        best = tune_plan(st["plan"], lambda st=st: st["op"].apply_block(st["out"]), key="block")
+        tuned[name] = {"group": best["group"], "engine": best["engine"],
+                       "candidates_ms": {str(c["group"]): round(c["ms"], 4) for c in best["candidates"]}}
 
     def timed(fn, steps, warmup):
         for _ in range(warmup):
@@ -322,7 +328,8 @@ def run_gato(args):
         "data": "synthetic (seeded water geometry and orbitals)",
         "config": {"workload": f"H2O HGH {N}^3 h={h} block Fock apply: 4 orbitals, 10 pair Poisson solves "
                                f"on the {2 * N}^3 doubled grid", "precision": "mixed", "N": N, "h": h,
-                   "n_occ": N_OCC, "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas"},
+                   "n_occ": N_OCC, "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas",
+                   "autotune": tuned},
         "clocks": clk.summary(),
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": host_in.numel() * 4,
                 "d2h_bytes_per_step": host_out.numel() * 4},

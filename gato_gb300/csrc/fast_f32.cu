@@ -55,5 +55,14 @@ int rows_inv<T>(int M, const PassArgs& a, int f0, int nfg, const T2* S1, const T
   return kNotHandled;
 }
 
+template <>
+int rows_inv_j<T>(int M, const PassArgs& a, int f0, int nfg, const T2* S1, const T2* tw, cudaStream_t s) {
+#define X(MM, A, B, L32, L64) \
+  case MM: return Launch<T, A, B, kF32 ? L32 : L64>::rows_inv_j(a, f0, nfg, S1, tw, s);
+  switch (M) { GATO_FAST_SHAPES(X) }
+#undef X
+  return kNotHandled;
+}
+
 }  // namespace fast
 }  // namespace gato

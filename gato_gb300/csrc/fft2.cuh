@@ -78,6 +78,65 @@ __device__ __forceinline__ void rdft(T2* v) {
   }
 }
 
+// The same DFT when only v[0 .. R/2) is nonzero (the zero-padded half of a
+// Hockney transform). For R = A B with A even the zeros are the upper half of
+// every inner A-point DFT, so the saving recurses down to the base radices.
+template <typename T2, int R, int DIR>
+__device__ __forceinline__ void rdft_half(T2* v) {
+  if constexpr (R == 2) {
+    v[1] = v[0];
+  } else if constexpr (R == 4) {
+    const T2 a = v[0], b = v[1];
+    const T2 ib = cmul_i(b, DIR);
+    v[0] = cadd(a, b);
+    v[1] = cadd(a, ib);
+    v[2] = csub(a, b);
+    v[3] = csub(a, ib);
+  } else if constexpr (R == 8) {
+    // even/odd split: E = DFT4(v0, v2, 0, 0), O = DFT4(v1, v3, 0, 0)
+    T2 e[4] = {v[0], v[2], v[0], v[0]}, o[4] = {v[1], v[3], v[1], v[1]};
+    rdft_half<T2, 4, DIR>(e);
+    rdft_half<T2, 4, DIR>(o);
+    using Rt = typename CT<T2>::R;
+    const Rt s = (Rt)0.70710678118654752440;
+    T2 w1, w3;
+    w1.x = s;
+    w1.y = (Rt)DIR * s;
+    w3.x = -s;
+    w3.y = (Rt)DIR * s;
+    o[1] = cmul(o[1], w1);
+    o[2] = cmul_i(o[2], DIR);
+    o[3] = cmul(o[3], w3);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      v[q] = cadd(e[q], o[q]);
+      v[q + 4] = csub(e[q], o[q]);
+    }
+  } else {
+    constexpr int A = Split<R>::A, B = Split<R>::B;
+    static_assert(A % 2 == 0, "half-input DFT needs an even inner radix");
+    T2 y[R];
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) {
+      T2 u[A];
+#pragma unroll
+      for (int n1 = 0; n1 < A / 2; ++n1) u[n1] = v[B * n1 + n2];
+      rdft_half<T2, A, DIR>(u);
+#pragma unroll
+      for (int k1 = 0; k1 < A; ++k1) y[n2 * A + k1] = ctw<T2, R, DIR>(u[k1], (n2 * k1) % R);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) {
+      T2 u[B];
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) u[n2] = y[n2 * A + k1];
+      rdft<T2, B, DIR>(u);
+#pragma unroll
+      for (int k2 = 0; k2 < B; ++k2) v[k1 + A * k2] = u[k2];
+    }
+  }
+}
+
 template <int R1, int R2> struct Shape {
   static constexpr int M = R1 * R2;
   static constexpr int RMAX = R1 > R2 ? R1 : R2;
@@ -101,7 +160,8 @@ __device__ __forceinline__ void fwd_stage1(T2* buf, int LP, int line, int n2, Ge
     if (!HALF || n1 < R1 / 2) v[n1] = get(R2 * n1 + n2);
     else v[n1].x = v[n1].y = 0;
   }
-  rdft<T2, R1, -1>(v);
+  if constexpr (HALF) rdft_half<T2, R1, -1>(v);
+  else rdft<T2, R1, -1>(v);
 #pragma unroll
   for (int k1 = 0; k1 < R1; ++k1) buf[(n2 * R1 + k1) * LP + line] = v[k1];
 }

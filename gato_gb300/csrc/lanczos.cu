@@ -159,9 +159,6 @@ __global__ void k_scale_copy(const T* __restrict__ src, T* dst, int64_t n, const
     dst[i] = (T)((double)src[i] * inv);
 }
 
-__global__ void k_copy_double(const double* src, double* dst) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) dst[0] = src[0];
-}
 
 // ---- tridiagonal eigensolver (FP64, one block) ----------------------------------
 

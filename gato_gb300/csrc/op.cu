@@ -4,7 +4,9 @@
 // apply      : stencil(+V) writes out; V_nl scatter-adds; the exchange pass
 //              subtracts sum_j phi_j J[phi_j psi] in its final z-row epilogue.
 // apply_block: F phi_i for every occupied orbital with the n(n+1)/2 pair
-//              potentials J[phi_i phi_j], each feeding both phi_i and phi_j.
+//              potentials J[phi_i phi_j], each feeding both phi_i and phi_j:
+//              the pipeline writes the J_ij fields, then one elementwise pass
+//              subtracts sum_j phi_j J_ij from every output (each J read once).
 // energy     : kinetic via the stencil's fused <phi, T phi> reduction (no
 //              store), V_ext and V_nl by reductions, E_H and E_x from one
 //              batched pair-solve pass in energy mode (rho with weight 1/2,
@@ -129,6 +131,7 @@ extern "C" int gato_op_destroy(gato_op_t op) {
   if (!op) return GATO_OK;
   cudaFree(op->dscratch);
   cudaFree(op->rho);
+  cudaFree(op->jbuf);
   delete op;
   return GATO_OK;
 }
@@ -175,6 +178,21 @@ extern "C" int gato_op_apply_block(gato_op_t op, void* out, void* stream) {
   if (op->nl) GATO_TRY(nonlocal_apply(op->nl->n, op->orbitals, out, op->n_orb, s));
   PassArgs a;
   block_pairs(a, *op, out, false);
+  if (poisson_j_supported(op->pp->p)) {
+    // pair potentials to J fields, then one elementwise pass: out_i -= sum_j phi_j J_ij
+    const size_t need = (size_t)2 * a.nf * op_n3(*op) * op_esize(*op);
+    if (op->jbuf_bytes < need) {
+      cudaFree(op->jbuf);
+      op->jbuf = nullptr;
+      op->jbuf_bytes = 0;
+      GATO_CUDA_TRY(cudaMalloc(&op->jbuf, need));
+      op->jbuf_bytes = need;
+    }
+    a.jbase = op->jbuf;
+    a.jstride = op_n3(*op);
+    GATO_TRY(poisson_run(op->pp->p, a, EPI_J, false, nullptr, s));
+    return pair_exchange(op->dtype, op->orbitals, op->n_orb, op->jbuf, out, op_n3(*op), s);
+  }
   return poisson_run(op->pp->p, a, EPI_ACC, true, nullptr, s);
 }
 

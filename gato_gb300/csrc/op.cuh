@@ -16,6 +16,8 @@ struct gato_operator {
   int n_orb = 0;
   double* dscratch = nullptr;   // small device doubles
   void* rho = nullptr;          // N^3 density scratch for the energy terms
+  void* jbuf = nullptr;         // pair potentials J_ij of the block apply
+  size_t jbuf_bytes = 0;
 };
 
 namespace gato {

@@ -325,10 +325,14 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
       GATO_TRY(fast::cols<T>(M, COL_FWD, S1, S2, gy, N, nfg, tw, nullptr, pl.H, s));
       GATO_TRY(fast::cols<T>(M, COL_FMI, S2, S2, gx, M, nfg, tw, (const T*)pl.ghat, pl.H, s));
       GATO_TRY(fast::cols<T>(M, COL_INV, S2, S1, gyi, N, nfg, tw, nullptr, pl.H, s));
-      GATO_TRY(fast::rows_inv<T>(M, args, f0, nfg, S1, tw, acc_here ? 1 : 0, epi == EPI_ENERGY, part,
-                                 sstride, s));
+      if (epi == EPI_J)
+        GATO_TRY(fast::rows_inv_j<T>(M, args, f0, nfg, S1, tw, s));
+      else
+        GATO_TRY(fast::rows_inv<T>(M, args, f0, nfg, S1, tw, acc_here ? 1 : 0, epi == EPI_ENERGY, part,
+                                   sstride, s));
       continue;
     }
+    if (epi == EPI_J) return fail(GATO_EUNSUPPORTED, "poisson: J output needs the register engine");
     // 1. z forward with the pair-density prologue
     k_rows_fwd<T><<<dim3((unsigned)((nrows + Lr - 1) / Lr), nfg), kFftThreads, sm_r, s>>>(
         args, f0, S1, pl.fp, tw, N, Lr);
@@ -576,3 +580,58 @@ extern "C" int gato_poisson_tune(gato_poisson_t plan, int group, int engine) {
   plan->p.engine = engine;
   return GATO_OK;
 }
+
+namespace gato {
+bool poisson_j_supported(const PoissonPlan& pl) {
+  if (pl.engine != 0) return false;
+  return (pl.dtype == GATO_F64 ? fast::rows_L<double>(pl.M) : fast::rows_L<float>(pl.M)) > 0;
+}
+
+namespace {
+// out_a -= sum over pairs (a, b) of phi_b J_ab (each J read once).
+template <typename T, int NORB>
+__global__ void k_pair_exchange(const T* __restrict__ orb, const T* __restrict__ J, T* out, int64_t n3) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n3;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    T phi[NORB], acc[NORB];
+#pragma unroll
+    for (int a = 0; a < NORB; ++a) {
+      phi[a] = orb[(int64_t)a * n3 + i];
+      acc[a] = (T)0;
+    }
+    int k = 0;
+#pragma unroll
+    for (int a = 0; a < NORB; ++a)
+#pragma unroll
+      for (int b = a; b < NORB; ++b, ++k) {
+        const T j = J[(int64_t)k * n3 + i];
+        acc[a] += phi[b] * j;
+        if (b != a) acc[b] += phi[a] * j;
+      }
+#pragma unroll
+    for (int a = 0; a < NORB; ++a) out[(int64_t)a * n3 + i] -= acc[a];
+  }
+}
+
+template <typename T>
+int pair_exchange_t(const T* orb, int n, const T* J, T* out, int64_t n3, cudaStream_t s) {
+  const unsigned g = grid_for(n3, 256, 152 * 8);
+  switch (n) {
+#define GATO_PX(NN) \
+  case NN: k_pair_exchange<T, NN><<<g, 256, 0, s>>>(orb, J, out, n3); break;
+    GATO_PX(1) GATO_PX(2) GATO_PX(3) GATO_PX(4) GATO_PX(5) GATO_PX(6) GATO_PX(7) GATO_PX(8)
+#undef GATO_PX
+    default: return fail(GATO_EUNSUPPORTED, "pair exchange: at most 8 orbitals");
+  }
+  GATO_LAUNCH_TRY();
+  return GATO_OK;
+}
+}  // namespace
+
+int pair_exchange(int dtype, const void* orbitals, int n, const void* J, void* out, int64_t n3,
+                  cudaStream_t s) {
+  if (dtype == GATO_F64)
+    return pair_exchange_t<double>((const double*)orbitals, n, (const double*)J, (double*)out, n3, s);
+  return pair_exchange_t<float>((const float*)orbitals, n, (const float*)J, (float*)out, n3, s);
+}
+}  // namespace gato

@@ -29,6 +29,10 @@ struct PassArgs {
   int nout = 0;
   int nf = 0;
   FieldDesc f[kMaxFields];
+  // EPI_J: part k (= 2 * field + {0: real, 1: imaginary}) of J is written to
+  // jbase + k * jstride
+  void* jbase = nullptr;
+  int64_t jstride = 0;
 };
 
 struct PoissonPlan {
@@ -47,7 +51,7 @@ struct PoissonPlan {
   int engine = 0;          // 0: register two-pass kernels where M allows, 1: generic Stockham
 };
 
-enum PoissonEpi { EPI_ACC = 0, EPI_ENERGY = 1 };
+enum PoissonEpi { EPI_ACC = 0, EPI_ENERGY = 1, EPI_J = 2 };
 
 enum ColMode { COL_FWD = 0, COL_INV = 1, COL_FMI = 2 };
 
@@ -83,7 +87,18 @@ template <typename T>
 int rows_inv(int M, const PassArgs& a, int f0, int nfg, const typename Cplx<T>::type* S1,
              const typename Cplx<T>::type* tw, int accumulate, bool energy, double* partials,
              int64_t slot_stride, cudaStream_t s);
+// z inverse writing the real and imaginary parts of J as separate fields (EPI_J).
+template <typename T>
+int rows_inv_j(int M, const PassArgs& a, int f0, int nfg, const typename Cplx<T>::type* S1,
+               const typename Cplx<T>::type* tw, cudaStream_t s);
 }  // namespace fast
+
+// out_a -= phi_b J_ab and out_b -= phi_a J_ab for every pair a <= b of n
+// fields, J_ab the k-th field of J in row-major pair order (0,0),(0,1),...
+int pair_exchange(int dtype, const void* orbitals, int n, const void* J, void* out, int64_t n3,
+                  cudaStream_t s);
+// True when the plan's size has register-engine kernels (EPI_J available).
+bool poisson_j_supported(const PoissonPlan& pl);
 
 // Runs every field of `args` through the pair-solve pipeline in groups of
 // at most plan.max_fields. EPI_ACC: out[o] = (accumulate ? out[o] : 0) +

@@ -15,7 +15,8 @@ __device__ __forceinline__ void load_tw(T2* tws, const T2* tw, int M) {
 }
 
 // Strided-line passes (y forward, x forward * kernel * x inverse, y inverse).
-template <typename T, int R1, int R2, int L, int MODE>
+// FULL: every CTA has L real columns (ncols % L == 0), so no per-access guard.
+template <typename T, int R1, int R2, int L, int MODE, bool FULL>
 __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
     k_cols(const typename Cplx<T>::type* in, typename Cplx<T>::type* out, ColGeom g,
            const typename Cplx<T>::type* tw, const T* ghat, int H) {
@@ -26,46 +27,55 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   T2* tws = buf + M * LP;
   load_tw(tws, tw, M);
   const int outer = blockIdx.x, col0 = blockIdx.y * L, f = blockIdx.z;
-  const int ncl = min(L, g.ncols - col0);
-  const T2* src = in + f * g.in_fs + outer * g.in_os + col0;
-  T2* dst = out + f * g.out_fs + outer * g.out_os + col0;
   const int t = threadIdx.x;
   const int line = t % L, q = t / L;   // q: n2 in stages 1/B, k1 in stages 2/A
+  const bool live = FULL || line < g.ncols - col0;
+  // per-thread bases: element (pos, line) of this CTA's tile is base[pos * ps]
+  const T2* src = in + f * g.in_fs + outer * g.in_os + col0 + line;
+  T2* dst = out + f * g.out_fs + outer * g.out_os + col0 + line;
+  const int64_t ips = g.in_ps, ops = g.out_ps;
   T2 X[R2];
   if (MODE != COL_INV) {
-    if (q < R2)
+    if (q < R2) {
+      const T2* b1 = src + q * ips;
       fwd_stage1<T2, R1, R2, true>(buf, LP, line, q, [&](int pos) {
         T2 v;
-        if (line < ncl) v = src[pos * g.in_ps + line];
+        if (live) v = b1[(pos - q) * ips];   // pos - q = R2 n1: a compile-time multiple of R2
         else v.x = v.y = 0;
         return v;
       });
+    }
     __syncthreads();
     if (q < R1) fwd_stage2<T2, R1, R2>(buf, LP, line, q, tws, X);
   } else {
     __syncthreads();
-    if (q < R1)
+    if (q < R1) {
+      const T2* b = src + q * ips;
 #pragma unroll
       for (int k2 = 0; k2 < R2; ++k2) {
-        if (line < ncl) X[k2] = src[(q + R1 * k2) * g.in_ps + line];
+        if (live) X[k2] = b[(int64_t)(R1 * k2) * ips];
         else X[k2].x = X[k2].y = 0;
       }
+    }
   }
   if (MODE == COL_FWD) {
-    if (q < R1 && line < ncl)
+    if (q < R1 && live) {
+      T2* b = dst + q * ops;
 #pragma unroll
-      for (int k2 = 0; k2 < R2; ++k2) dst[(q + R1 * k2) * g.out_ps + line] = X[k2];
+      for (int k2 = 0; k2 < R2; ++k2) b[(int64_t)(R1 * k2) * ops] = X[k2];
+    }
     return;
   }
   if (MODE == COL_FMI && q < R1) {
     const int ky = outer, kyo = ky <= M - ky ? ky : M - ky;
     const int kz = col0 + line, kzo = kz <= M - kz ? kz : M - kz;
     const T* gp = ghat + (int64_t)kyo * H + kzo;
+    const int64_t HH = (int64_t)H * H;
 #pragma unroll
     for (int k2 = 0; k2 < R2; ++k2) {
       const int kx = q + R1 * k2;
       const int kxo = kx <= M - kx ? kx : M - kx;
-      const T gv = line < ncl ? gp[(int64_t)kxo * H * H] : (T)0;
+      const T gv = live ? gp[kxo * HH] : (T)0;
       X[k2].x *= gv;
       X[k2].y *= gv;
     }
@@ -73,21 +83,24 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   __syncthreads();   // stage-2 reads of buf are complete
   if (q < R1) inv_stageA<T2, R1, R2>(buf, LP, line, q, tws, X);
   __syncthreads();
-  if (q < R2)
+  if (q < R2) {
+    T2* b = dst + q * ops;
     inv_stageB<T2, R1, R2, true>(buf, LP, line, q, [&](int pos, T2 v) {
-      if (line < ncl) dst[pos * g.out_ps + line] = v;
+      if (live) b[(pos - q) * ops] = v;
     });
+  }
 }
 
-// z forward with the pair-density prologue.
+// z forward with the pair-density prologue. One shared buffer: each thread
+// holds its stage inputs in registers across the barrier that separates the
+// reads of one stage from the writes of the next.
 template <typename T, int R1, int R2, int L>
 __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
     k_rows_fwd(PassArgs args, int f0, typename Cplx<T>::type* S1, const typename Cplx<T>::type* tw) {
   using T2 = typename Cplx<T>::type;
   constexpr int M = R1 * R2, N = M / 2, LP = L + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
-  T2* stg = reinterpret_cast<T2*>(smraw);
-  T2* buf = stg + M * LP;
+  T2* buf = reinterpret_cast<T2*>(smraw);
   T2* tws = buf + M * LP;
   load_tw(tws, tw, M);
   const int p = blockIdx.y;
@@ -104,47 +117,61 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
       v.x = dens<T>(fd.p[0], args.in, gi);
       if (fd.p[1].a >= 0) v.y = dens<T>(fd.p[1], args.in, gi);
     }
-    stg[z * LP + line] = v;
+    buf[z * LP + line] = v;
   }
   __syncthreads();
   const int t = threadIdx.x, line = t % L, q = t / L;
-  if (q < R2) fwd_stage1<T2, R1, R2, true>(buf, LP, line, q, [&](int pos) { return stg[pos * LP + line]; });
+  T2 v[R1];
+  if (q < R2) {
+#pragma unroll
+    for (int n1 = 0; n1 < R1 / 2; ++n1) v[n1] = buf[(R2 * n1 + q) * LP + line];
+    rdft_half<T2, R1, -1>(v);
+  }
+  __syncthreads();
+  if (q < R2)
+#pragma unroll
+    for (int k1 = 0; k1 < R1; ++k1) buf[(q * R1 + k1) * LP + line] = v[k1];
   __syncthreads();
   T2 X[R2];
-  if (q < R1) {
-    fwd_stage2<T2, R1, R2>(buf, LP, line, q, tws, X);
+  if (q < R1) fwd_stage2<T2, R1, R2>(buf, LP, line, q, tws, X);
+  __syncthreads();
+  if (q < R1)
 #pragma unroll
-    for (int k2 = 0; k2 < R2; ++k2) stg[(q + R1 * k2) * LP + line] = X[k2];
-  }
+    for (int k2 = 0; k2 < R2; ++k2) buf[(q + R1 * k2) * LP + line] = X[k2];
   __syncthreads();
   T2* dst = S1 + (int64_t)p * nrows * M;
   for (int i = threadIdx.x; i < L * M; i += blockDim.x) {
     const int ln = i / M, kz = i % M;
     const int64_t r = row0 + ln;
-    if (r < nrows) dst[r * M + kz] = stg[kz * LP + ln];
+    if (r < nrows) dst[r * M + kz] = buf[kz * LP + ln];
   }
 }
 
-// z inverse over every field of the group, then the epilogue of poisson.cu.
-template <typename T, int R1, int R2, int L, bool ENERGY>
+// z inverse over every field of the group, then the epilogue. NO > 0: the
+// accumulation terms target outputs < NO, kept in registers (each thread owns
+// EPT fixed (row, z) elements); NO == 0: energy mode.
+template <typename T, int R1, int R2, int L, int NO>
 __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
     k_rows_inv(PassArgs args, int f0, int nfg, const typename Cplx<T>::type* S1,
                const typename Cplx<T>::type* tw, int accumulate, double* partials,
                int64_t slot_stride) {
   using T2 = typename Cplx<T>::type;
   constexpr int M = R1 * R2, N = M / 2, LP = L + 1;
+  constexpr int NT = L * Shape<R1, R2>::RMAX;
+  constexpr int EPT = (L * N + NT - 1) / NT;
+  constexpr bool ENERGY = NO == 0;
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ double sh[32];
-  T2* stg = reinterpret_cast<T2*>(smraw);
-  T2* buf = stg + M * LP;
+  T2* buf = reinterpret_cast<T2*>(smraw);
   T2* tws = buf + M * LP;
-  T* acc = reinterpret_cast<T*>(tws + M);
   load_tw(tws, tw, M);
   const int64_t row0 = (int64_t)blockIdx.x * L;
   const int64_t nrows = (int64_t)N * N;
-  const int nout = args.nout;
-  if (!ENERGY)
-    for (int i = threadIdx.x; i < nout * L * N; i += blockDim.x) acc[i] = (T)0;
+  T acc[ENERGY ? 1 : NO][EPT];
+#pragma unroll
+  for (int o = 0; o < (ENERGY ? 1 : NO); ++o)
+#pragma unroll
+    for (int e = 0; e < EPT; ++e) acc[o][e] = (T)0;
   Acc<T> e0, e1;
   const int t = threadIdx.x, line = t % L, q = t / L;
   for (int p = 0; p < nfg; ++p) {
@@ -157,31 +184,43 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
       T2 v;
       if (r < nrows) v = src[r * M + kz];
       else v.x = v.y = 0;
-      stg[kz * LP + ln] = v;
+      buf[kz * LP + ln] = v;
     }
     __syncthreads();
+    T2 X[R2];
     if (q < R1) {
-      T2 X[R2];
 #pragma unroll
-      for (int k2 = 0; k2 < R2; ++k2) X[k2] = stg[(q + R1 * k2) * LP + line];
-      inv_stageA<T2, R1, R2>(buf, LP, line, q, tws, X);
+      for (int k2 = 0; k2 < R2; ++k2) X[k2] = buf[(q + R1 * k2) * LP + line];
+    }
+    __syncthreads();
+    if (q < R1) inv_stageA<T2, R1, R2>(buf, LP, line, q, tws, X);
+    __syncthreads();
+    T2 w[R1];
+    if (q < R2) {
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) w[k1] = buf[(q * R1 + k1) * LP + line];
+      rdft<T2, R1, +1>(w);
     }
     __syncthreads();
     if (q < R2)
-      inv_stageB<T2, R1, R2, true>(buf, LP, line, q, [&](int pos, T2 v) { stg[pos * LP + line] = v; });
+#pragma unroll
+      for (int n1 = 0; n1 < R1 / 2; ++n1) buf[(q + R2 * n1) * LP + line] = w[n1];
     __syncthreads();
-    for (int i = threadIdx.x; i < L * N; i += blockDim.x) {
+#pragma unroll
+    for (int e = 0; e < EPT; ++e) {
+      const int i = e * NT + t;
+      if (i >= L * N) break;
       const int ln = i / N, z = i % N;
       const int64_t r = row0 + ln;
       if (r >= nrows) continue;
       const int64_t gi = r * N + z;
-      const T2 J = stg[z * LP + ln];
+      const T2 J = buf[z * LP + ln];
 #pragma unroll
       for (int qq = 0; qq < 2; ++qq) {
         const PartDesc& d = fd.p[qq];
         if (d.a < 0) continue;
         const T val = qq == 0 ? J.x : J.y;
-        if (ENERGY) {
+        if constexpr (ENERGY) {
           const T de = dens<T>(d, args.in, gi);
           if (d.eslot == 0) e0.add_prod(de * (T)d.ew, val);
           else e1.add_prod(de * (T)d.ew, val);
@@ -189,13 +228,16 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
           for (int k = 0; k < d.nt; ++k) {
             T m = (T)d.coef[k];
             if (d.tc[k] >= 0) m *= reinterpret_cast<const T*>(args.in[d.tc[k]])[gi];
-            acc[(d.to[k] * L + ln) * N + z] += m * val;
+            const int to = d.to[k];
+#pragma unroll
+            for (int o = 0; o < NO; ++o)
+              if (o == to) acc[o][e] += m * val;
           }
         }
       }
     }
   }
-  if (ENERGY) {
+  if constexpr (ENERGY) {
     const double s0 = block_sum(e0.value(), sh);
     const double s1 = block_sum(e1.value(), sh);
     if (threadIdx.x == 0) {
@@ -203,18 +245,79 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
       partials[slot_stride + blockIdx.x] = s1;
     }
   } else {
-    __syncthreads();
-    for (int o = 0; o < nout; ++o) {
+    const int nout = args.nout;
+#pragma unroll
+    for (int o = 0; o < NO; ++o) {
+      if (o >= nout) break;
       T* dst = reinterpret_cast<T*>(args.out[o]);
-      for (int i = threadIdx.x; i < L * N; i += blockDim.x) {
+#pragma unroll
+      for (int e = 0; e < EPT; ++e) {
+        const int i = e * NT + t;
+        if (i >= L * N) break;
         const int ln = i / N, z = i % N;
         const int64_t r = row0 + ln;
         if (r >= nrows) continue;
         const int64_t gi = r * N + z;
-        const T v = acc[(o * L + ln) * N + z];
-        dst[gi] = accumulate ? dst[gi] + v : v;
+        dst[gi] = accumulate ? dst[gi] + acc[o][e] : acc[o][e];
       }
     }
+  }
+}
+
+// z inverse of one field per CTA (grid.y = field), writing J_re and J_im of
+// the row block to their own real fields (the EPI_J epilogue).
+template <typename T, int R1, int R2, int L>
+__global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
+    k_rows_inv_j(T* jbase, int64_t jstride, int f0, const typename Cplx<T>::type* S1,
+                 const typename Cplx<T>::type* tw) {
+  using T2 = typename Cplx<T>::type;
+  constexpr int M = R1 * R2, N = M / 2, LP = L + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T2* buf = reinterpret_cast<T2*>(smraw);
+  T2* tws = buf + M * LP;
+  load_tw(tws, tw, M);
+  const int p = blockIdx.y;
+  const int64_t row0 = (int64_t)blockIdx.x * L;
+  const int64_t nrows = (int64_t)N * N;
+  const T2* src = S1 + (int64_t)p * nrows * M;
+  for (int i = threadIdx.x; i < L * M; i += blockDim.x) {
+    const int ln = i / M, kz = i % M;
+    const int64_t r = row0 + ln;
+    T2 v;
+    if (r < nrows) v = src[r * M + kz];
+    else v.x = v.y = 0;
+    buf[kz * LP + ln] = v;
+  }
+  __syncthreads();
+  const int t = threadIdx.x, line = t % L, q = t / L;
+  T2 X[R2];
+  if (q < R1) {
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) X[k2] = buf[(q + R1 * k2) * LP + line];
+  }
+  __syncthreads();
+  if (q < R1) inv_stageA<T2, R1, R2>(buf, LP, line, q, tws, X);
+  __syncthreads();
+  T2 w[R1];
+  if (q < R2) {
+#pragma unroll
+    for (int k1 = 0; k1 < R1; ++k1) w[k1] = buf[(q * R1 + k1) * LP + line];
+    rdft<T2, R1, +1>(w);
+  }
+  __syncthreads();
+  if (q < R2)
+#pragma unroll
+    for (int n1 = 0; n1 < R1 / 2; ++n1) buf[(q + R2 * n1) * LP + line] = w[n1];
+  __syncthreads();
+  T* jre = jbase + (int64_t)(2 * (f0 + p)) * jstride;
+  T* jim = jre + jstride;
+  for (int i = threadIdx.x; i < L * N; i += blockDim.x) {
+    const int ln = i / N, z = i % N;
+    const int64_t r = row0 + ln;
+    if (r >= nrows) continue;
+    const T2 J = buf[z * LP + ln];
+    jre[r * N + z] = J.x;
+    jim[r * N + z] = J.y;
   }
 }
 
@@ -230,49 +333,64 @@ struct Launch {
   using T2 = typename Cplx<T>::type;
   static constexpr int M = R1 * R2, N = M / 2, NT = L * Shape<R1, R2>::RMAX;
   static size_t sm_cols() { return (size_t)(M * (L + 1) + M) * sizeof(T2); }
-  static size_t sm_rows(int nout) {
-    return (size_t)(2 * M * (L + 1) + M) * sizeof(T2) + (size_t)nout * L * N * sizeof(T);
-  }
+  static size_t sm_rows() { return (size_t)(M * (L + 1) + M) * sizeof(T2); }
   static int cols(int mode, const T2* in, T2* out, const ColGeom& g, int outer, int nf, const T2* tw,
                   const T* ghat, int H, cudaStream_t s) {
+    if (g.ncols % L == 0) return cols_t<true>(mode, in, out, g, outer, nf, tw, ghat, H, s);
+    return cols_t<false>(mode, in, out, g, outer, nf, tw, ghat, H, s);
+  }
+  template <bool FULL>
+  static int cols_t(int mode, const T2* in, T2* out, const ColGeom& g, int outer, int nf, const T2* tw,
+                    const T* ghat, int H, cudaStream_t s) {
     dim3 grid(outer, (g.ncols + L - 1) / L, nf);
     const size_t sm = sm_cols();
     if (mode == COL_FWD) {
-      GATO_TRY(smem_attr(k_cols<T, R1, R2, L, COL_FWD>, sm));
-      k_cols<T, R1, R2, L, COL_FWD><<<grid, NT, sm, s>>>(in, out, g, tw, ghat, H);
+      GATO_TRY(smem_attr(k_cols<T, R1, R2, L, COL_FWD, FULL>, sm));
+      k_cols<T, R1, R2, L, COL_FWD, FULL><<<grid, NT, sm, s>>>(in, out, g, tw, ghat, H);
     } else if (mode == COL_INV) {
-      GATO_TRY(smem_attr(k_cols<T, R1, R2, L, COL_INV>, sm));
-      k_cols<T, R1, R2, L, COL_INV><<<grid, NT, sm, s>>>(in, out, g, tw, ghat, H);
+      GATO_TRY(smem_attr(k_cols<T, R1, R2, L, COL_INV, FULL>, sm));
+      k_cols<T, R1, R2, L, COL_INV, FULL><<<grid, NT, sm, s>>>(in, out, g, tw, ghat, H);
     } else {
-      GATO_TRY(smem_attr(k_cols<T, R1, R2, L, COL_FMI>, sm));
-      k_cols<T, R1, R2, L, COL_FMI><<<grid, NT, sm, s>>>(in, out, g, tw, ghat, H);
+      GATO_TRY(smem_attr(k_cols<T, R1, R2, L, COL_FMI, FULL>, sm));
+      k_cols<T, R1, R2, L, COL_FMI, FULL><<<grid, NT, sm, s>>>(in, out, g, tw, ghat, H);
     }
     GATO_LAUNCH_TRY();
     return GATO_OK;
   }
   static int rows_fwd(const PassArgs& a, int f0, int nfg, T2* S1, const T2* tw, cudaStream_t s) {
-    const size_t sm = sm_rows(0);
+    const size_t sm = sm_rows();
     GATO_TRY(smem_attr(k_rows_fwd<T, R1, R2, L>, sm));
     const int64_t nrows = (int64_t)N * N;
     k_rows_fwd<T, R1, R2, L><<<dim3((unsigned)((nrows + L - 1) / L), nfg), NT, sm, s>>>(a, f0, S1, tw);
     GATO_LAUNCH_TRY();
     return GATO_OK;
   }
-  static int rows_inv(const PassArgs& a, int f0, int nfg, const T2* S1, const T2* tw, int accumulate,
-                      bool energy, double* partials, int64_t slot_stride, cudaStream_t s) {
-    const size_t sm = sm_rows(energy ? 0 : a.nout);
+  template <int NO>
+  static int rows_inv_no(const PassArgs& a, int f0, int nfg, const T2* S1, const T2* tw, int accumulate,
+                         double* partials, int64_t slot_stride, cudaStream_t s) {
+    const size_t sm = sm_rows();
     const unsigned nblk = (unsigned)(((int64_t)N * N + L - 1) / L);
-    if (energy) {
-      GATO_TRY(smem_attr(k_rows_inv<T, R1, R2, L, true>, sm));
-      k_rows_inv<T, R1, R2, L, true><<<nblk, NT, sm, s>>>(a, f0, nfg, S1, tw, accumulate, partials,
-                                                          slot_stride);
-    } else {
-      GATO_TRY(smem_attr(k_rows_inv<T, R1, R2, L, false>, sm));
-      k_rows_inv<T, R1, R2, L, false><<<nblk, NT, sm, s>>>(a, f0, nfg, S1, tw, accumulate, partials,
-                                                           slot_stride);
-    }
+    GATO_TRY(smem_attr(k_rows_inv<T, R1, R2, L, NO>, sm));
+    k_rows_inv<T, R1, R2, L, NO><<<nblk, NT, sm, s>>>(a, f0, nfg, S1, tw, accumulate, partials,
+                                                       slot_stride);
     GATO_LAUNCH_TRY();
     return GATO_OK;
+  }
+  static int rows_inv_j(const PassArgs& a, int f0, int nfg, const T2* S1, const T2* tw, cudaStream_t s) {
+    const size_t sm = sm_rows();
+    const unsigned nblk = (unsigned)(((int64_t)N * N + L - 1) / L);
+    GATO_TRY(smem_attr(k_rows_inv_j<T, R1, R2, L>, sm));
+    k_rows_inv_j<T, R1, R2, L><<<dim3(nblk, nfg), NT, sm, s>>>((T*)a.jbase, a.jstride, f0, S1, tw);
+    GATO_LAUNCH_TRY();
+    return GATO_OK;
+  }
+  static int rows_inv(const PassArgs& a, int f0, int nfg, const T2* S1, const T2* tw, int accumulate,
+                      bool energy, double* partials, int64_t slot_stride, cudaStream_t s) {
+    if (energy) return rows_inv_no<0>(a, f0, nfg, S1, tw, accumulate, partials, slot_stride, s);
+    if (a.nout <= 1) return rows_inv_no<1>(a, f0, nfg, S1, tw, accumulate, partials, slot_stride, s);
+    if (a.nout <= 2) return rows_inv_no<2>(a, f0, nfg, S1, tw, accumulate, partials, slot_stride, s);
+    if (a.nout <= 4) return rows_inv_no<4>(a, f0, nfg, S1, tw, accumulate, partials, slot_stride, s);
+    return rows_inv_no<8>(a, f0, nfg, S1, tw, accumulate, partials, slot_stride, s);
   }
 };
 

@@ -162,6 +162,17 @@ __global__ void __launch_bounds__(kBZ* kTY)
 
   Acc<T> acc;
   const int gz = z0 + tz;
+  // V of the next output plane, loaded one iteration ahead so its latency
+  // overlaps the barrier and the plane wait.
+  T vn[kYPT];
+  auto load_v = [&](int xo) {
+#pragma unroll
+    for (int k = 0; k < kYPT; ++k) {
+      const int gy = y0 + ty + k * kTY;
+      vn[k] = (V && xo < xe && gy < ny && gz < nz) ? V[((int64_t)xo * ny + gy) * nz + gz] : (T)0;
+    }
+  };
+  load_v(xs);
   for (int q = 0; q < P; ++q) {
     const int s = q % kSlots;
     mbar_wait_bounded(&bars[s], (uint32_t)((q / kSlots) & 1), err, 101);
@@ -191,11 +202,12 @@ __global__ void __launch_bounds__(kBZ* kTY)
         T val = coef * lap_combine<T>(ctr, s1, s2, c, R);
         if (gy < ny && gz < nz) {
           const int64_t gi = (int64_t)b * bstride + ((int64_t)xo * ny + gy) * nz + gz;
-          if (V) val += V[((int64_t)xo * ny + gy) * nz + gz] * ctr;
+          if (V) val += vn[k] * ctr;
           if (out) out[gi] = val;
           if (dot_part) acc.add_prod(ctr, val);
         }
       }
+      load_v(xo + 1);
     }
     __syncthreads();  // every thread is done with plane q - R
     if (tid == 0 && q >= R && q - R + kSlots < P) issue(q - R + kSlots);
