@@ -37,6 +37,7 @@ _SIGS = {
     "gato_last_error": [C.c_char_p, C.c_size_t],
     "gato_device_status": [P_i32, vp],
     "gato_dot": [i32, vp, vp, i64, f64, vp, vp],
+    "gato_dot_noalloc": [i32, vp, vp, i64, f64, vp, vp],
     "gato_normalize": [i32, vp, i64, vp, vp],
     "gato_stencil_apply": [i32, vp, vp, vp, i32, i32, i32, i32, f64, i32, i32, vp, f64, vp],
     "gato_softened_coulomb": [i32, vp, i32, f64, i32, P_f64, P_f64, f64, vp],
