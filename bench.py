@@ -353,8 +353,124 @@ def run_gato(args):
         dist.destroy_process_group()
 
 
+def _sync_time(fn):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = fn()
+    torch.cuda.synchronize()
+    return r, time.perf_counter() - t0
+
+
+def run_workload(args):
+    """Configuration workloads (one JSON line each); the headline metric is the default run."""
+    import numpy as np
+    import torch
+
+    from gato_gb300.grid import Grid3D
+    out = {"workload": args.workload}
+    if args.workload == "c1":
+        # hydrogen 64^3, L = 20, 7-point Laplacian, softened Coulomb a = 0.1, Lanczos m = 80, K = 1
+        from gato_gb300.hamiltonian import Hamiltonian
+        from gato_gb300.potentials import softened_coulomb
+        from gato_gb300.solvers.lanczos import lanczos
+        g = Grid3D(64, 20.0)
+        psi0 = np.random.default_rng(0).uniform(0.0, 1.0, g.shape)
+        for prec, dt in (("fp64", torch.float64), ("mixed", torch.float32)):
+            H = Hamiltonian(g, softened_coulomb(g, 1.0, 0.1, dtype=dt), order=2)
+            p = torch.tensor(psi0, device="cuda", dtype=dt)
+            lanczos(H, p, 80, 1)
+            res, dt_s = _sync_time(lambda: lanczos(H, p, 80, 1))
+            out[prec] = {"E0": float(res.eigenvalues[0]), "lanczos_s": dt_s}
+        out["abs_dE0"] = abs(out["mixed"]["E0"] - out["fp64"]["E0"])
+    elif args.workload == "c2":
+        # helium RHF 96^3, L = 16, Z = 2, softening 0.1, Gaussian + 1e-3 noise, mixing 0.5, tol 1e-8
+        from gato_gb300.potentials import softened_coulomb
+        from gato_gb300.scf import scf_rhf
+        g = Grid3D(96, 16.0)
+        X, Y, Z = (a.cpu().numpy() for a in g.coords())
+        phi0 = np.exp(-(X * X + Y * Y + Z * Z)) + 1e-3 * np.random.default_rng(3).standard_normal(g.shape)
+        for prec, dt in (("mixed", torch.float32), ("fp64", torch.float64)):
+            r, t = _sync_time(lambda: scf_rhf(softened_coulomb(g, 2.0, 0.1), g, 1,
+                                              initial_orbitals=torch.tensor(phi0, device="cuda", dtype=dt)[..., None],
+                                              max_iters=30, tol=1e-8, mixing=0.5, order=4, epsilon=0.1,
+                                              precision=prec))
+            out[prec] = {"E": r.energy, "iters": r.n_iters, "converged": r.converged, "scf_s": t}
+        out["abs_dE"] = abs(out["mixed"]["E"] - out["fp64"]["E"])
+    elif args.workload in ("c3", "c4"):
+        from gato_gb300.physics.water import (bo_energy, hellmann_feynman_force, optimize_water_geometry,
+                                              solve_rhf_at_geometry, water_hgh_elements, water_initial_geometry)
+        from gato_gb300.scf import to_fields
+        N, h = args.N, H_DEFAULT
+        g = Grid3D(N, N * h)
+        el = water_hgh_elements()
+        rng = np.random.default_rng(11)
+        if args.workload == "c3":
+            nuc = water_initial_geometry(1.81, 104.5)
+            nuc = type(nuc)(nuc.positions + torch.tensor(rng.uniform(-0.05, 0.05, (3, 3))), nuc.charges)
+            p32, t32 = _sync_time(lambda: solve_rhf_at_geometry(nuc, el, g, precision="mixed", tol=1e-8,
+                                                                max_iters=80))
+            out["mixed"] = {"E": p32.energy, "iters": p32.n_iters, "converged": p32.converged, "scf_s": t32,
+                            "orbital_energies": p32.orbital_energies.cpu().tolist()}
+            # FP64 continuation from the mixed fixed point: same converged state if the paths agree
+            p64, t64 = _sync_time(lambda: solve_rhf_at_geometry(
+                nuc, el, g, precision="fp64", tol=1e-8, max_iters=args.fp64_iters,
+                initial_orbitals=to_fields(p32.orbitals).to(torch.float64).permute(1, 2, 3, 0)))
+            out["fp64_continuation"] = {"E": p64.energy, "iters": p64.n_iters, "converged": p64.converged,
+                                        "scf_s": t64}
+            out["abs_dE"] = abs(p32.energy - p64.energy)
+        else:
+            R, ang = rng.uniform(1.5, 2.3), rng.uniform(90.0, 130.0)
+            nuc = water_initial_geometry(R, ang)
+            steps, worst, fd_ms = [], 0.0, 0.0
+            d = 1e-3
+
+            def fd_check(point):
+                nonlocal worst, fd_ms
+                F = hellmann_feynman_force(point, el, g).numpy()
+                o64 = to_fields(point.orbitals).to(torch.float64).permute(1, 2, 3, 0)
+                t0 = time.perf_counter()
+                for a in range(3):
+                    for c in range(3):
+                        pp, pm = point.nuclei.positions.clone(), point.nuclei.positions.clone()
+                        pp[a, c] += d
+                        pm[a, c] -= d
+                        fd = -(float(bo_energy(pp, point.nuclei.charges, o64, el, g))
+                               - float(bo_energy(pm, point.nuclei.charges, o64, el, g))) / (2 * d)
+                        worst = max(worst, abs(F[a, c] - fd))
+                fd_ms += 1e3 * (time.perf_counter() - t0)
+
+            from gato_gb300.geometry_opt import optimize_geometry_alternating
+            from gato_gb300.physics.water import bo_grad_positions
+
+            def solve_at(nuclei, prev):
+                return solve_rhf_at_geometry(nuclei, el, g, precision="mixed",
+                                             initial_orbitals=prev.orbitals if prev is not None else None)
+
+            def on_step(step, p):
+                steps.append(p.energy)
+                if step % args.fd_every == 0 or step == args.geom_steps - 1:
+                    fd_check(p)
+            (final, traj), t = _sync_time(lambda: optimize_geometry_alternating(
+                nuc, solve_at_geometry=solve_at, learning_rate=0.02, geom_steps=args.geom_steps,
+                bo_grad=lambda p: bo_grad_positions(p.nuclei.positions, p.nuclei.charges, p.orbitals, el, g),
+                on_step=on_step))
+            _, tf = _sync_time(lambda: hellmann_feynman_force(final, el, g))
+            out.update({"geom_steps": args.geom_steps, "opt_s_including_fd_checks": t,
+                        "fd_check_s": fd_ms / 1e3, "E_first_last": [traj[0].energy, final.energy],
+                        "max_abs_force_minus_fd_Ha_per_bohr": worst, "force_ms_mixed": 1e3 * tf,
+                        "scf_iters_per_step": [p.n_iters for p in traj[1:]],
+                        "final_R_OH": float(torch.linalg.norm(final.nuclei.positions[1] - final.nuclei.positions[0]))})
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default=None, choices=["c1", "c2", "c3", "c4"],
+                    help="run a configuration workload instead of the headline metric")
+    ap.add_argument("--fp64-iters", type=int, default=3)
+    ap.add_argument("--geom-steps", type=int, default=60)
+    ap.add_argument("--fd-every", type=int, default=20)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
@@ -364,7 +480,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.workload:
+        run_workload(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gato(args)

@@ -58,6 +58,7 @@ _SIGS = {
     "gato_exchange_apply": [vp, vp, vp, i32, vp, f64, vp],
     "gato_axpby": [i32, vp, vp, vp, i64, f64, f64, vp],
     "gato_field_sum": [i32, vp, i32, i64, vp, vp],
+    "gato_convert": [i32, vp, i32, vp, i64, vp],
     "gato_op_create": [i32, i32, f64, i32, i32, C.POINTER(vp)],
     "gato_op_destroy": [vp],
     "gato_op_set_potential": [vp, vp],

@@ -275,3 +275,29 @@ extern "C" int gato_field_sum(int dtype, const void* fields, int nf, int64_t n, 
   GATO_LAUNCH_TRY();
   return GATO_OK;
 }
+
+namespace gato {
+template <typename S, typename D>
+__global__ void k_convert(const S* __restrict__ src, D* dst, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (D)src[i];
+}
+}  // namespace gato
+
+extern "C" int gato_convert(int src_dtype, const void* src, int dst_dtype, void* dst, int64_t n,
+                            void* stream) {
+  if (!src || !dst || n <= 0) return fail(GATO_EBADARG, "gato_convert: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  const unsigned g = grid_for(n, 256);
+  if (src_dtype == GATO_F64 && dst_dtype == GATO_F32)
+    k_convert<double, float><<<g, 256, 0, s>>>((const double*)src, (float*)dst, n);
+  else if (src_dtype == GATO_F32 && dst_dtype == GATO_F64)
+    k_convert<float, double><<<g, 256, 0, s>>>((const float*)src, (double*)dst, n);
+  else if (src_dtype == dst_dtype)
+    GATO_CUDA_TRY(cudaMemcpyAsync(dst, src, n * (src_dtype == GATO_F64 ? 8 : 4), cudaMemcpyDeviceToDevice, s));
+  else
+    return fail(GATO_EBADARG, "gato_convert: bad dtypes %d -> %d", src_dtype, dst_dtype);
+  GATO_LAUNCH_TRY();
+  return GATO_OK;
+}

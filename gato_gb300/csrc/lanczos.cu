@@ -59,8 +59,12 @@ __device__ __forceinline__ T pre_load(const T* W, const Pre<T>& p, const T* sc, 
   return w;
 }
 
-// c_k partials: part[k * nblk + block] = sum_i V_k[i] w[i]
-template <typename T>
+// c_k partials: part[k * nblk + block] = sum_i V_k[i] w[i]. C is the type the
+// per-vector products and warp sums run in; the launches use the field type:
+// c_k is a cancellation sum (nearly orthogonal vectors), so its error scales
+// with |w|, not with c_k, and FP32 products would leave 1e-9-level components
+// in an FP64 basis.
+template <typename T, typename C>
 __global__ void __launch_bounds__(kLzThreads)
     k_gemv_t(const T* __restrict__ V, int64_t ld, int nk, const T* __restrict__ W, Pre<T> pre,
              int64_t n, double* part) {
@@ -71,22 +75,22 @@ __global__ void __launch_bounds__(kLzThreads)
   for (int i = threadIdx.x; i < nw * nk; i += blockDim.x) wacc[i] = 0.0;
   __syncthreads();
   for (int64_t base = (int64_t)blockIdx.x * kChunk; base < n; base += (int64_t)gridDim.x * kChunk) {
-    T w[kEPT];
+    C w[kEPT];
 #pragma unroll
     for (int e = 0; e < kEPT; ++e) {
       const int64_t i = base + e * kLzThreads + threadIdx.x;
-      w[e] = i < n ? pre_load(W, pre, sc, i) : (T)0;
+      w[e] = i < n ? (C)pre_load(W, pre, sc, i) : (C)0;
     }
     for (int k = 0; k < nk; ++k) {
       const T* vk = V + (int64_t)k * ld;
-      T s = (T)0;
+      C s = (C)0;
 #pragma unroll
       for (int e = 0; e < kEPT; ++e) {
         const int64_t i = base + e * kLzThreads + threadIdx.x;
-        if (i < n) s = fma(vk[i], w[e], s);
+        if (i < n) s = fma((C)vk[i], w[e], s);
       }
       double d;
-      if constexpr (sizeof(T) == 4) d = (double)warp_sumf(s);
+      if constexpr (sizeof(C) == 4) d = (double)warp_sumf(s);
       else d = warp_sum(s);
       if (lane == 0) wacc[warp * nk + k] += d;
     }
@@ -99,8 +103,13 @@ __global__ void __launch_bounds__(kLzThreads)
   }
 }
 
-// W <- W - pre - sum_k c_k v_k ; norm partials part[block]
-template <typename T>
+// W <- W - pre - sum_k c_k v_k ; norm partials part[block]. The correction
+// sum_k c_k v_k is formed in C and subtracted in T. Launched with C = float:
+// once the three-term part is removed the c_k are roundoff-sized (about
+// 1e-14 |w| in FP64), so rounding each term to FP32 perturbs w far below its
+// own last digit, while GB300's narrow FP64 pipe would otherwise spend one
+// DFMA per element per basis vector here.
+template <typename T, typename C>
 __global__ void __launch_bounds__(kLzThreads)
     k_gemv_n(const T* __restrict__ V, int64_t ld, int nk, T* __restrict__ W, Pre<T> pre,
              const double* __restrict__ c, int64_t n, double* part) {
@@ -113,24 +122,27 @@ __global__ void __launch_bounds__(kLzThreads)
   Acc<T> acc;
   for (int64_t base = (int64_t)blockIdx.x * kChunk; base < n; base += (int64_t)gridDim.x * kChunk) {
     T w[kEPT];
+    C corr[kEPT];
 #pragma unroll
     for (int e = 0; e < kEPT; ++e) {
       const int64_t i = base + e * kLzThreads + threadIdx.x;
       w[e] = i < n ? pre_load(W, pre, sc, i) : (T)0;
+      corr[e] = (C)0;
     }
     for (int k = 0; k < nk; ++k) {
       const T* vk = V + (int64_t)k * ld;
-      const T ck = (T)cs[k];
+      const C ck = (C)cs[k];
 #pragma unroll
       for (int e = 0; e < kEPT; ++e) {
         const int64_t i = base + e * kLzThreads + threadIdx.x;
-        if (i < n) w[e] -= ck * vk[i];
+        if (i < n) corr[e] = fma(ck, (C)vk[i], corr[e]);
       }
     }
 #pragma unroll
     for (int e = 0; e < kEPT; ++e) {
       const int64_t i = base + e * kLzThreads + threadIdx.x;
       if (i < n) {
+        w[e] -= (T)corr[e];
         W[i] = w[e];
         acc.add_prod(w[e], w[e]);
       }
@@ -397,9 +409,9 @@ int lz_step(T* Vb, int64_t n, double dV, int j, int passes, double* alphas, doub
   const size_t smt = (size_t)(kLzThreads / 32) * nk * sizeof(double);
   const size_t smn = (size_t)nk * sizeof(double);
   if (smt > 48 * 1024)
-    GATO_CUDA_TRY(cudaFuncSetAttribute(k_gemv_t<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt));
+    GATO_CUDA_TRY(cudaFuncSetAttribute(k_gemv_t<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt));
   // alpha_j = dV <v_j, w'>
-  k_gemv_t<T><<<z.nblk, kLzThreads, (kLzThreads / 32) * sizeof(double), s>>>(vj, n, 1, W, p1, n, z.part);
+  k_gemv_t<T, T><<<z.nblk, kLzThreads, (kLzThreads / 32) * sizeof(double), s>>>(vj, n, 1, W, p1, n, z.part);
   GATO_LAUNCH_TRY();
   GATO_TRY(finalize_sums(z.part, 1, z.nblk, dV, alphas + j, s));
   Pre<T> p2 = p1;
@@ -407,10 +419,10 @@ int lz_step(T* Vb, int64_t n, double dV, int j, int passes, double* alphas, doub
   p2.s[1] = alphas + j;
   for (int p = 0; p < passes; ++p) {
     const Pre<T>& pp = p == 0 ? p2 : Pre<T>();
-    k_gemv_t<T><<<z.nblk, kLzThreads, smt, s>>>(Vb, n, nk, W, pp, n, z.part);
+    k_gemv_t<T, T><<<z.nblk, kLzThreads, smt, s>>>(Vb, n, nk, W, pp, n, z.part);
     GATO_LAUNCH_TRY();
     GATO_TRY(finalize_sums(z.part, nk, z.nblk, dV, z.coef, s));
-    k_gemv_n<T><<<z.nblk, kLzThreads, smn, s>>>(Vb, n, nk, W, pp, z.coef, n, z.part);
+    k_gemv_n<T, float><<<z.nblk, kLzThreads, smn, s>>>(Vb, n, nk, W, pp, z.coef, n, z.part);
     GATO_LAUNCH_TRY();
   }
   GATO_TRY(finalize_sums(z.part, 1, z.nblk, dV, z.nrm, s));

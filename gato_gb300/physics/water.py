@@ -73,7 +73,8 @@ def solve_rhf_at_geometry(nuclei: Nuclei, elements, grid: Grid3D, *, max_iters: 
                           initial_orbitals=None, precision: str = "fp64") -> WaterPoint:
     """RHF on a fixed geometry with HGH pseudopotentials (water.py:129-174)."""
     dtype = precision_dtype(precision)
-    V_local = hgh_local_potential(nuclei, elements, grid, dtype)
+    # V_loc stays FP64: the SCF evaluates the energy in FP64 under either precision
+    V_local = hgh_local_potential(nuclei, elements, grid, torch.float64)
     V_nl = nonlocal_for(nuclei, elements, grid, dtype)
     n_electrons = int(total_valence_charge(elements))
     if n_electrons % 2 != 0:

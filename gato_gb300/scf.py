@@ -2,9 +2,10 @@
 
 Orbitals are stored field-major, (n, N, N, N); the reference's (N, N, N, n)
 arrays are the ``permute(1, 2, 3, 0)`` view of that storage, and both forms
-are accepted. ``precision="mixed"`` runs the fields, stencils, FFTs and
-exchange in FP32 with FP64 / float-float reductions, FP64 Lanczos
-coefficients and an FP64 tridiagonal eigensolve; ``"fp64"`` is the plain path.
+are accepted. ``precision="mixed"`` runs the Fock operator (stencils, FFTs, exchange) and
+the Lanczos vectors in FP32 with FP64 / float-float reductions, FP64 Lanczos
+coefficients and an FP64 tridiagonal eigensolve, and keeps the SCF density,
+V_H and the energy in FP64; ``"fp64"`` is the plain path.
 """
 from __future__ import annotations
 
@@ -292,17 +293,29 @@ def scf_rhf(V_ext, grid: Grid3D, n_occ: int, *, initial_orbitals=None, max_iters
     (seeded with the sum of the current orbitals), linear density mixing,
     the energy of the new orbitals, and the |E_k - E_{k-1}| < tol test in FP64
     on the host. Everything between the two host reads runs on the device.
+
+    With ``precision="mixed"`` the Fock operator, its exchange and the
+    eigensolve run on FP32 fields; the density, the mixing, V_H and the energy
+    run in FP64 on an FP64 copy of the new orbitals. An FP32 Hartree solve
+    carries a relative error near 1e-7 in E_H (about 2e-6 Ha for water), which
+    would be larger than the 1e-6 Ha agreement the two precisions are held
+    to; the FP64 part costs one FP64 density solve and one FP64 energy pass
+    per iteration against about m FP32 Fock applies.
     """
     dtype = precision_dtype(precision)
+    mixed = dtype != torch.float64
+    f64 = torch.float64
     dev = _lib.require_cuda()
     dc = _lib.dtype_code(dtype)
     eps = grid.h / 2 if epsilon is None else epsilon
     m = default_krylov_dim(grid.N, n_occ) if lanczos_iters is None else int(lanczos_iters)
     K = min(n_occ, m)
+    V_ext64 = as_field(V_ext, f64)
     V_ext = as_field(V_ext, dtype)
     nl = _native_nl(V_nl_apply, grid, dtype)
     generic_nl = V_nl_apply is not None and nl is None
     plan = get_plan(grid.N, grid.h, eps, dtype, pair_fields(n_occ))
+    plan64 = get_plan(grid.N, grid.h, eps, f64, pair_fields(n_occ))
     if initial_orbitals is None:
         orb = _default_initial_orbitals(V_ext, grid, n_occ, boundary, order, m, dtype, reorth_passes)
     else:
@@ -311,25 +324,36 @@ def scf_rhf(V_ext, grid: Grid3D, n_occ: int, *, initial_orbitals=None, max_iters
     n3 = grid.N ** 3
     s = lambda: C.c_void_p(_lib.stream())   # noqa: E731
     P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
-    rho = _density_fields(orb)
+
+    def convert(src, dst):
+        _lib.call("gato_convert", _lib.dtype_code(src), P(src), _lib.dtype_code(dst), P(dst), src.numel(), s())
+        return dst
+
+    orb64 = convert(orb, torch.empty(orb.shape, dtype=f64, device=dev)) if mixed else orb
+    rho = _density_fields(orb64)
     rho_new = torch.empty_like(rho)
     V_H = torch.empty_like(rho)
-    V_tot = torch.empty_like(rho)
-    seed = torch.empty_like(rho)
+    V_tot64 = torch.empty_like(rho)
+    V_tot = torch.empty(grid.shape, dtype=dtype, device=dev) if mixed else V_tot64
+    seed = torch.empty(grid.shape, dtype=dtype, device=dev)
     krylov = torch.empty((m + 1,) + grid.shape, dtype=dtype, device=dev)
     bufs = [torch.empty((K,) + grid.shape, dtype=dtype, device=dev) for _ in range(2)]
     op = Operator(grid, dtype, order, boundary)
     op.set_nonlocal(nl)
+    op64 = Operator(grid, f64, order, boundary) if mixed else op
+    buf64 = torch.empty((K,) + grid.shape, dtype=f64, device=dev) if mixed else None
     history: list[float] = []
     E_prev = float("inf")
     E = float("inf")
-    orbital_energies = torch.zeros(n_occ, dtype=torch.float64, device=dev)
+    orbital_energies = torch.zeros(n_occ, dtype=f64, device=dev)
     converged = False
     terms = None
     it = 0
     for it in range(1, max_iters + 1):
-        plan.potential(rho, out=V_H)
-        _lib.call("gato_axpby", dc, P(V_ext), P(V_H), P(V_tot), n3, 1.0, 1.0, s())
+        plan64.potential(rho, out=V_H)
+        _lib.call("gato_axpby", _lib.F64, P(V_ext64), P(V_H), P(V_tot64), n3, 1.0, 1.0, s())
+        if mixed:
+            convert(V_tot64, V_tot)
         op.set_potential(V_tot)
         op.set_exchange(plan, orb)
         _lib.call("gato_field_sum", dc, P(orb), orb.shape[0], n3, P(seed), s())
@@ -342,10 +366,11 @@ def scf_rhf(V_ext, grid: Grid3D, n_occ: int, *, initial_orbitals=None, max_iters
             res = lanczos(_Bound(grid, op), seed, n_iters=m, n_eigenstates=n_occ, krylov=krylov, out=new,
                           reorth_passes=reorth_passes)
         orbital_energies = res.eigenvalues
-        _density_fields(new, rho_new)
-        _lib.call("gato_mix", dc, P(rho), P(rho_new), n3, float(mixing), s())
         orb = new
-        terms = _energy_terms(orb, V_ext, grid, boundary, order, eps, V_nl_apply, op=op)
+        orb64 = convert(orb, buf64[: orb.shape[0]]) if mixed else orb
+        _density_fields(orb64, rho_new)
+        _lib.call("gato_mix", _lib.F64, P(rho), P(rho_new), n3, float(mixing), s())
+        terms = _energy_terms(orb64, V_ext64, grid, boundary, order, eps, V_nl_apply, op=op64)
         E = float(terms.sum())
         history.append(E)
         if abs(E - E_prev) < tol:

@@ -147,6 +147,9 @@ int gato_mix(int dtype, void* rho, const void* rho_new, int64_t npts, double a, 
  * elementwise combination the SCF loop needs.                            */
 int gato_axpby(int dtype, const void* x, const void* y, void* out, int64_t npts, double a, double b,
                void* stream);
+/* dst = (dst dtype) src, n elements: the precision changes between the FP32
+ * Fock applies and the FP64 density / Hartree / energy of the mixed SCF.    */
+int gato_convert(int src_dtype, const void* src, int dst_dtype, void* dst, int64_t n, void* stream);
 /* out = sum_k fields[k]: the Lanczos seed sum(orbitals, axis=-1) (scf.py:417). */
 int gato_field_sum(int dtype, const void* fields, int nf, int64_t npts, void* out, void* stream);
 /* out += coef * K psi, K psi = sum_j phi_j J[phi_j psi]: scf.py:66-85.     */

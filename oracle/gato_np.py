@@ -579,6 +579,12 @@ def lanczos(H, psi0, n_iters=80, n_eigenstates=4, tol=1e-10):   # lanczos.py:110
         off = betas[: n_iters - 1]
         T = T + np.diag(off, 1) + np.diag(off, -1)
     evals, evecs = np.linalg.eigh(T)
+    # LAPACK leaves each eigenvector's sign arbitrary (the reference inherits its
+    # platform's choice); fix it as the device solver does: the component of
+    # largest magnitude is positive. Energies and densities do not depend on
+    # it; the SCF seed sum(orbitals) does.
+    idx = np.argmax(np.abs(evecs), axis=0)
+    evecs = evecs * np.where(evecs[idx, np.arange(evecs.shape[1])] < 0, -1.0, 1.0)
     K = min(n_eigenstates, n_iters)
     V_stack = Vb[:n_iters].reshape(n_iters, -1)
     psi_states = (evecs[:, :K].T @ V_stack).reshape(K, *shape)
