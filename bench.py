@@ -464,6 +464,49 @@ def run_workload(args):
     print(json.dumps(out), flush=True)
 
 
+def run_profile(args):
+    """The block (or matvec) Fock apply alone, for ncu: no autotune sweep, no FP64, no CPU leg.
+
+    One launch group spans every pair field (what the autotuner picks at 128^3).
+    Prints one JSON line with the kernel launches of one step.
+    """
+    import torch
+
+    from gato_gb300 import _lib
+    from gato_gb300.autotune import set_plan
+    from gato_gb300.geometry import Nuclei
+    from gato_gb300.grid import Grid3D
+    from gato_gb300.physics.water import water_hgh_elements
+    from gato_gb300.pseudopotentials import hgh_local_potential, nonlocal_for
+    from gato_gb300.scf import Operator, _density_fields, pair_fields
+    from gato_gb300.solvers.poisson import get_plan
+
+    dtype = torch.float32 if args.profile_dtype == "f32" else torch.float64
+    N, h = args.N, H_DEFAULT
+    g = Grid3D(N, N * h)
+    pos, orbs = synthetic_water(N, h)
+    nuc = Nuclei(torch.tensor(pos), torch.tensor([8.0, 1.0, 1.0], dtype=torch.float64))
+    el = water_hgh_elements()
+    fields = torch.tensor(orbs, device="cuda").to(dtype).contiguous()
+    plan = get_plan(N, h, h / 2, dtype, pair_fields(N_OCC))
+    set_plan(plan, plan.max_fields)
+    op = Operator(g, dtype, 4, "dirichlet")
+    op.set_potential((hgh_local_potential(nuc, el, g, dtype) + plan.potential(_density_fields(fields))).contiguous())
+    op.set_nonlocal(nonlocal_for(nuc, el, g, dtype))
+    op.set_exchange(plan, fields)
+    out = torch.empty_like(fields)
+    step = (lambda: op.apply_block(out)) if args.profile == "block" else (lambda: op.apply(fields[0], out[0]))
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    n0 = _lib.launch_count()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": args.profile, "dtype": args.profile_dtype, "N": N, "steps": args.steps,
+                      "launches_per_step": (_lib.launch_count() - n0) / args.steps}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default=None, choices=["c1", "c2", "c3", "c4"],
@@ -477,10 +520,15 @@ def main():
     ap.add_argument("--impl", default="gato", choices=["gato", "reference"])
     ap.add_argument("--N", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--profile", default=None, choices=["block", "matvec"],
+                    help="run only the block / matvec Fock apply (for ncu captures)")
+    ap.add_argument("--profile-dtype", default="f32", choices=["f32", "f64"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.workload:
+    if args.profile:
+        run_profile(args)
+    elif args.workload:
         run_workload(args)
     elif args.impl == "reference":
         run_reference(args)

@@ -1,16 +1,22 @@
 // Finite-difference Laplacian / Hamiltonian apply (operators.py:40-130,
 // hamiltonian.py:25-31).
 //
-// Hot path (Dirichlet, 16-byte aligned rows): each CTA owns a 16 (y) x 32 (z)
+// Hot path (Dirichlet, 16-byte aligned rows): each CTA owns a 32 (y) x 32 (z)
 // column of the grid and marches along x through a chunk of planes. One
 // elected thread streams (16+2R) x (32+2A) halo planes into an 8-slot
 // shared-memory ring with TMA (cp.async.bulk.tensor, mbarrier completion);
 // the tensor map's zero out-of-bounds fill is exactly the reference's zero
 // padding, so no boundary branches exist. x-neighbours live in a per-thread
 // register queue, y/z neighbours are read from the centre plane in shared
-// memory. V and the output are plain coalesced accesses. HBM-bound: the
-// algorithmic traffic is 3 N^3 s bytes (psi, V, out).
+// memory. The 16 x 32 V tile of each centre plane rides in the same ring slot
+// (a second tensor map, same mbarrier), so V arrives with the ring's
+// look-ahead instead of one DRAM round trip per plane; the output is a plain
+// coalesced store. HBM-bound: the algorithmic traffic is 3 N^3 s bytes
+// (psi, V, out).
 #include <cuda.h>
+
+#include <algorithm>
+#include <cstring>
 
 #include "common.cuh"
 #include "ptx.cuh"
@@ -101,10 +107,10 @@ __global__ void k_stencil_generic(const T* __restrict__ psi, const T* __restrict
 
 // ---- TMA plane-marching kernel ---------------------------------------------------
 constexpr int kBZ = 32;       // tile width along z (one warp)
-constexpr int kBY = 16;       // tile height along y
-constexpr int kTY = 8;        // thread rows: each thread owns kBY/kTY points
+constexpr int kBY = 32;       // tile height along y
+constexpr int kTY = 8;        // thread rows; each thread owns kYPT consecutive y rows
 constexpr int kYPT = kBY / kTY;
-constexpr int kSlots = 8;     // plane ring depth
+constexpr int kSlots = 6;     // plane ring depth: 3 planes of look-ahead, 3 FP32 (2 FP64) CTAs per SM
 
 template <typename T, int R>
 struct TmaGeom {
@@ -112,15 +118,25 @@ struct TmaGeom {
   static constexpr int PW = kBZ + 2 * A;
   static constexpr int PH = kBY + 2 * R;
   static constexpr int BOX_BYTES = PW * PH * (int)sizeof(T);
-  static constexpr int SLOT_BYTES = (BOX_BYTES + 127) / 128 * 128;
+  static constexpr int V_OFF = (BOX_BYTES + 127) / 128 * 128;   // V tile inside the slot
+  static constexpr int V_BYTES = kBZ * kBY * (int)sizeof(T);
+  static constexpr int SLOT_BYTES = V_OFF + (V_BYTES + 127) / 128 * 128;
   static constexpr int SMEM = kSlots * SLOT_BYTES + kSlots * 8 + 128;
 };
 
-template <typename T, int R>
+// One CTA: a kBY x kBZ column of one field, planes [xs, xs + cx) along x.
+// Plane q of the chunk is x = xs - R + q and sits in ring slot q % kSlots; it
+// feeds the x register queue at iteration q and is the centre plane at
+// iteration q + R, after which its slot is refilled with plane q + kSlots.
+// The plane loop is unrolled by the ring depth, so slot addresses are
+// immediates and the queue shifts are register renames. Each thread owns
+// rows yt .. yt + kYPT - 1 at z = tz: its y neighbours are its own queue
+// centres plus 2R halo rows, its z neighbours are shared-memory reads.
+template <typename T, int R, bool HAS_V, bool STORE, bool DOT>
 __global__ void __launch_bounds__(kBZ* kTY)
-    k_stencil_tma(const __grid_constant__ CUtensorMap tmap, const T* __restrict__ V,
-                  T* __restrict__ out, int nx, int ny, int nz, int cx, int tiles_z,
-                  int64_t bstride, T coef, double* dot_part, int* err) {
+    k_stencil_tma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap vmap,
+                  T* __restrict__ out, int nx, int ny, int nz, int cx, int tiles_z, int64_t bstride,
+                  T coef, double* dot_part, int* err) {
   using G = TmaGeom<T, R>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* smem =
@@ -144,75 +160,101 @@ __global__ void __launch_bounds__(kBZ* kTY)
   }
   __syncthreads();
 
+  // Only the centre planes R <= q < P - R carry a V tile.
   auto issue = [&](int q) {
-    int s = q % kSlots;
-    mbar_expect_tx(&bars[s], G::BOX_BYTES);
+    const int s = q % kSlots;
+    const bool v = HAS_V && q >= R && q < P - R;
+    mbar_expect_tx(&bars[s], G::BOX_BYTES + (v ? G::V_BYTES : 0));
     tma_load_4d(smem + s * G::SLOT_BYTES, &tmap, &bars[s], z0 - G::A, y0 - R, xs - R + q, b);
+    if (v) tma_load_3d(smem + s * G::SLOT_BYTES + G::V_OFF, &vmap, &bars[s], z0, y0, xs - R + q);
   };
+  int issued = 0;   // meaningful in thread 0 only
   if (tid == 0) {
-    int n0 = P < kSlots ? P : kSlots;
-    for (int q = 0; q < n0; ++q) issue(q);
+    issued = P < kSlots ? P : kSlots;
+    for (int q = 0; q < issued; ++q) issue(q);
   }
+
+  const int yt = ty * kYPT;
+  const int gz = z0 + tz;
+  unsigned live = 0;
+#pragma unroll
+  for (int k = 0; k < kYPT; ++k)
+    if (gz < nz && y0 + yt + k < ny) live |= 1u << k;
+  T* obase = nullptr;
+  if (STORE) obase = out + (int64_t)b * bstride + ((int64_t)xs * ny + (y0 + yt)) * nz + gz;
+  const int64_t pstride = (int64_t)ny * nz;
+  const int cidx = (yt + R) * G::PW + tz + G::A;   // this thread's first row, centre column
 
   T xq[kYPT][2 * R + 1];
 #pragma unroll
   for (int k = 0; k < kYPT; ++k)
 #pragma unroll
     for (int r = 0; r < 2 * R + 1; ++r) xq[k][r] = (T)0;
-
   Acc<T> acc;
-  const int gz = z0 + tz;
-  // V of the next output plane, loaded one iteration ahead so its latency
-  // overlaps the barrier and the plane wait.
-  T vn[kYPT];
-  auto load_v = [&](int xo) {
+  bool bad = false;
+  int q = 0;
+  for (int qb = 0; qb < P && !bad; qb += kSlots) {
 #pragma unroll
-    for (int k = 0; k < kYPT; ++k) {
-      const int gy = y0 + ty + k * kTY;
-      vn[k] = (V && xo < xe && gy < ny && gz < nz) ? V[((int64_t)xo * ny + gy) * nz + gz] : (T)0;
-    }
-  };
-  load_v(xs);
-  for (int q = 0; q < P; ++q) {
-    const int s = q % kSlots;
-    mbar_wait_bounded(&bars[s], (uint32_t)((q / kSlots) & 1), err, 101);
-    const T* pl = reinterpret_cast<const T*>(smem + s * G::SLOT_BYTES);
-#pragma unroll
-    for (int k = 0; k < kYPT; ++k) {
-      const int y = ty + k * kTY;
-#pragma unroll
-      for (int r = 0; r < 2 * R; ++r) xq[k][r] = xq[k][r + 1];
-      xq[k][2 * R] = pl[(y + R) * G::PW + (tz + G::A)];
-    }
-    if (q >= 2 * R) {
-      const int xo = xs + q - 2 * R;
-      const T* pc = reinterpret_cast<const T*>(smem + ((q - R) % kSlots) * G::SLOT_BYTES);
+    for (int j = 0; j < kSlots; ++j) {
+      q = qb + j;
+      if (q >= P) break;
+      if (!mbar_wait_bounded(&bars[j], (uint32_t)((qb / kSlots) & 1), err, 101)) bad = true;
+      const T* pl = reinterpret_cast<const T*>(smem + j * G::SLOT_BYTES);
 #pragma unroll
       for (int k = 0; k < kYPT; ++k) {
-        const int y = ty + k * kTY;
-        const int gy = y0 + y;
-        const int idx = (y + R) * G::PW + (tz + G::A);
-        const T ctr = xq[k][R];
-        T s1 = xq[k][R - 1] + xq[k][R + 1] + pc[idx - G::PW] + pc[idx + G::PW] + pc[idx - 1] +
-               pc[idx + 1];
-        T s2 = (T)0;
-        if constexpr (R == 2)
-          s2 = xq[k][0] + xq[k][4] + pc[idx - 2 * G::PW] + pc[idx + 2 * G::PW] + pc[idx - 2] +
-               pc[idx + 2];
-        T val = coef * lap_combine<T>(ctr, s1, s2, c, R);
-        if (gy < ny && gz < nz) {
-          const int64_t gi = (int64_t)b * bstride + ((int64_t)xo * ny + gy) * nz + gz;
-          if (V) val += vn[k] * ctr;
-          if (out) out[gi] = val;
-          if (dot_part) acc.add_prod(ctr, val);
+#pragma unroll
+        for (int r = 0; r < 2 * R; ++r) xq[k][r] = xq[k][r + 1];
+        xq[k][2 * R] = pl[cidx + k * G::PW];
+      }
+      if (q >= 2 * R) {
+        const int cs = (j + kSlots - R) % kSlots;   // compile-time after unrolling
+        const T* pc = reinterpret_cast<const T*>(smem + cs * G::SLOT_BYTES);
+        const T* pv = reinterpret_cast<const T*>(smem + cs * G::SLOT_BYTES + G::V_OFF);
+        T col[kYPT + 2 * R];
+#pragma unroll
+        for (int i = 0; i < R; ++i) {
+          col[i] = pc[cidx + (i - R) * G::PW];
+          col[R + kYPT + i] = pc[cidx + (kYPT + i) * G::PW];
+        }
+#pragma unroll
+        for (int k = 0; k < kYPT; ++k) col[R + k] = xq[k][R];
+        T* op = STORE ? obase + (int64_t)(q - 2 * R) * pstride : nullptr;
+#pragma unroll
+        for (int k = 0; k < kYPT; ++k) {
+          const int idx = cidx + k * G::PW;
+          const T ctr = xq[k][R];
+          T s1 = xq[k][R - 1] + xq[k][R + 1] + col[R + k - 1] + col[R + k + 1] + pc[idx - 1] +
+                 pc[idx + 1];
+          T s2 = (T)0;
+          if constexpr (R == 2)
+            s2 = xq[k][0] + xq[k][4] + col[k] + col[k + 4] + pc[idx - 2] + pc[idx + 2];
+          T val = coef * lap_combine<T>(ctr, s1, s2, c, R);
+          if constexpr (HAS_V) val += pv[(yt + k) * kBZ + tz] * ctr;
+          if (live & (1u << k)) {
+            if constexpr (STORE) op[k * nz] = val;
+            if constexpr (DOT) acc.add_prod(ctr, val);
+          }
         }
       }
-      load_v(xo + 1);
+      // every thread is done with plane q - R; a timed-out wait anywhere stops the CTA
+      if (__syncthreads_or(bad)) {
+        bad = true;
+        break;
+      }
+      if (tid == 0 && q >= R && q - R + kSlots < P) {
+        issue(q - R + kSlots);
+        ++issued;
+      }
     }
-    __syncthreads();  // every thread is done with plane q - R
-    if (tid == 0 && q >= R && q - R + kSlots < P) issue(q - R + kSlots);
   }
-  if (dot_part) {
+  if (bad) {
+    // drain the copies still in flight (bounded) before the CTA's shared memory goes away
+    if (tid == 0)
+      for (int p = q; p < issued; ++p)
+        mbar_wait_bounded(&bars[p % kSlots], (uint32_t)((p / kSlots) & 1), err, 102);
+    return;
+  }
+  if constexpr (DOT) {
     double v = block_sum(acc.value(), sh);
     if (tid == 0)
       dot_part[(int64_t)b * gridDim.x * gridDim.y + (int64_t)blockIdx.y * gridDim.x + blockIdx.x] =
@@ -220,10 +262,46 @@ __global__ void __launch_bounds__(kBZ* kTY)
   }
 }
 
+// Resident CTAs of a kernel on the whole GPU (occupancy x SMs).
+template <typename K>
+int resident_ctas(K kernel, int smem) {
+  int dev = 0, sms = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kBZ * kTY, smem) != cudaSuccess ||
+      per <= 0)
+    return 152;
+  return per * sms;
+}
+
+template <typename T, int R, bool HAS_V, bool STORE, bool DOT>
+int launch_tma_mode(const CUtensorMap& tm, const CUtensorMap& vm, void* out, int nb, int nx, int ny,
+                    int nz, int64_t bstride, double coef, double* dot_part, int* nparts,
+                    cudaStream_t s) {
+  using G = TmaGeom<T, R>;
+  auto kern = k_stencil_tma<T, R, HAS_V, STORE, DOT>;
+  GATO_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM));
+  const int tiles_z = (nz + kBZ - 1) / kBZ, tiles_y = (ny + kBY - 1) / kBY;
+  const int tiles = tiles_z * tiles_y;
+  // Split x into chunks so the grid is one full resident wave where the
+  // problem allows (every CTA streams at once, no tail wave); a chunk keeps at
+  // least 4 planes, since its 2R halo planes are re-read.
+  static const int cap = resident_ctas(kern, G::SMEM);   // one value per instantiation
+  int chunks = (int)std::max<int64_t>(1, cap / ((int64_t)tiles * nb));
+  chunks = std::min(chunks, std::max(1, nx / 4));
+  const int cx = (nx + chunks - 1) / chunks;
+  chunks = (nx + cx - 1) / cx;
+  dim3 grid(tiles, chunks, nb), block(kBZ, kTY);
+  if (nparts) *nparts = tiles * chunks;
+  kern<<<grid, block, G::SMEM, s>>>(tm, vm, (T*)out, nx, ny, nz, cx, tiles_z, bstride, (T)coef,
+                                    dot_part, device_error_word());
+  GATO_LAUNCH_TRY();
+  return GATO_OK;
+}
+
 template <typename T, int R>
 int launch_tma(const void* psi, const void* V, void* out, int nb, int nx, int ny, int nz,
                int64_t bstride, double coef, double* dot_part, int* nparts, cudaStream_t s) {
-  using G = TmaGeom<T, R>;
   alignas(64) unsigned char tm[128];
   TmaBox box;
   box.rank = 4;
@@ -234,27 +312,45 @@ int launch_tma(const void* psi, const void* V, void* out, int nb, int nx, int ny
   box.strides_bytes[0] = (uint64_t)nz * sizeof(T);
   box.strides_bytes[1] = (uint64_t)ny * nz * sizeof(T);
   box.strides_bytes[2] = (uint64_t)bstride * sizeof(T);
-  box.box[0] = G::PW;
-  box.box[1] = G::PH;
+  box.box[0] = TmaGeom<T, R>::PW;
+  box.box[1] = TmaGeom<T, R>::PH;
   box.box[2] = 1;
   box.box[3] = 1;
   GATO_TRY(encode_tma(tm, sizeof(T) == 8 ? GATO_F64 : GATO_F32, psi, box));
-  const int tiles_z = (nz + kBZ - 1) / kBZ, tiles_y = (ny + kBY - 1) / kBY;
-  const int tiles = tiles_z * tiles_y;
-  // Chunk length along x: enough CTAs to fill 152 SMs about three deep,
-  // but no chunk shorter than 8 planes (the 2R halo planes are overhead).
-  int cx = nx;
-  while (cx > 8 && (int64_t)tiles * ((nx + cx - 1) / cx) * nb < 3 * 152) cx = (cx + 1) / 2;
-  const int chunks = (nx + cx - 1) / cx;
-  GATO_CUDA_TRY(cudaFuncSetAttribute(k_stencil_tma<T, R>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM));
-  dim3 grid(tiles, chunks, nb), block(kBZ, kTY);
-  if (nparts) *nparts = tiles * chunks;
-  k_stencil_tma<T, R><<<grid, block, G::SMEM, s>>>(
-      *reinterpret_cast<const CUtensorMap*>(tm), (const T*)V, (T*)out, nx, ny, nz, cx, tiles_z,
-      bstride, (T)coef, dot_part, device_error_word());
-  GATO_LAUNCH_TRY();
-  return GATO_OK;
+  alignas(64) unsigned char vm[128] = {};
+  if (V) {
+    TmaBox vb;
+    vb.rank = 3;
+    vb.dims[0] = nz;
+    vb.dims[1] = ny;
+    vb.dims[2] = nx;
+    vb.strides_bytes[0] = (uint64_t)nz * sizeof(T);
+    vb.strides_bytes[1] = (uint64_t)ny * nz * sizeof(T);
+    vb.box[0] = kBZ;
+    vb.box[1] = kBY;
+    vb.box[2] = 1;
+    GATO_TRY(encode_tma(vm, sizeof(T) == 8 ? GATO_F64 : GATO_F32, V, vb));
+  } else {
+    memcpy(vm, tm, sizeof(vm));   // never read without V
+  }
+  const CUtensorMap& T4 = *reinterpret_cast<const CUtensorMap*>(tm);
+  const CUtensorMap& V3 = *reinterpret_cast<const CUtensorMap*>(vm);
+  const int mode = (V ? 4 : 0) | (out ? 2 : 0) | (dot_part ? 1 : 0);
+#define GATO_TMA_MODE(M, HV, ST, DT)                                                          \
+  case M:                                                                                    \
+    return launch_tma_mode<T, R, HV, ST, DT>(T4, V3, out, nb, nx, ny, nz, bstride, coef,     \
+                                             dot_part, nparts, s);
+  switch (mode) {
+    GATO_TMA_MODE(1, false, false, true)
+    GATO_TMA_MODE(2, false, true, false)
+    GATO_TMA_MODE(3, false, true, true)
+    GATO_TMA_MODE(5, true, false, true)
+    GATO_TMA_MODE(6, true, true, false)
+    GATO_TMA_MODE(7, true, true, true)
+    default:
+      return fail(GATO_EBADARG, "stencil: nothing to compute");
+  }
+#undef GATO_TMA_MODE
 }
 
 template <typename T>
@@ -263,7 +359,7 @@ int stencil_typed(const void* psi, const void* V, void* out, int nb, int nx, int
                   double dv, cudaStream_t s) {
   const bool tma_ok = boundary == GATO_DIRICHLET && ((uint64_t)nz * sizeof(T)) % 16 == 0 &&
                       ((uint64_t)bstride * sizeof(T)) % 16 == 0 &&
-                      ((uintptr_t)psi % 16) == 0 && nb <= 65535;
+                      ((uintptr_t)psi % 16) == 0 && ((uintptr_t)V % 16) == 0 && nb <= 65535;
   double* part = nullptr;
   if (dot_dev) {
     // worst case: generic path uses kRedBlocks partials per batch.
