@@ -34,6 +34,21 @@ template <typename T2, int R, int DIR>
 __device__ __forceinline__ T2 ctw(T2 a, int e) {
   using Rt = typename CT<T2>::R;
   if (e == 0) return a;
+  if ((4 * e) % R == 0) {   // a quarter-turn multiple: -1 or +-i, exact sign and swap
+    const int k = 4 * e / R;
+    T2 r;
+    if (k == 2) {
+      r.x = -a.x;
+      r.y = -a.y;
+    } else if ((k == 1) == (DIR > 0)) {   // * i
+      r.x = -a.y;
+      r.y = a.x;
+    } else {                              // * -i
+      r.x = a.y;
+      r.y = -a.x;
+    }
+    return r;
+  }
   const Rt c = (Rt)TwC<R>::c(e);
   const Rt s = (Rt)DIR * (Rt)TwC<R>::s(e);
   T2 r;

@@ -67,15 +67,17 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
     return;
   }
   if (MODE == COL_FMI && q < R1) {
+    static_assert(R2 % 2 == 0, "the octant fold below splits k2 at R2 / 2");
     const int ky = outer, kyo = ky <= M - ky ? ky : M - ky;
     const int kz = col0 + line, kzo = kz <= M - kz ? kz : M - kz;
-    const T* gp = ghat + (int64_t)kyo * H + kzo;
-    const int64_t HH = (int64_t)H * H;
+    const int64_t HH = (int64_t)H * H, st = (int64_t)R1 * HH;
+    // kx = q + R1 k2 (q < R1): k2 < R2/2 gives kx <= M/2, read at kx; the upper
+    // half folds to M - kx = (M - q) - R1 k2.
+    const T* glo = ghat + (int64_t)q * HH + (int64_t)kyo * H + kzo;
+    const T* ghi = ghat + (int64_t)(M - q) * HH + (int64_t)kyo * H + kzo;
 #pragma unroll
     for (int k2 = 0; k2 < R2; ++k2) {
-      const int kx = q + R1 * k2;
-      const int kxo = kx <= M - kx ? kx : M - kx;
-      const T gv = live ? gp[kxo * HH] : (T)0;
+      const T gv = live ? (k2 < R2 / 2 ? glo[k2 * st] : ghi[-k2 * st]) : (T)0;
       X[k2].x *= gv;
       X[k2].y *= gv;
     }
@@ -103,21 +105,39 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   T2* buf = reinterpret_cast<T2*>(smraw);
   T2* tws = buf + M * LP;
   load_tw(tws, tw, M);
+  constexpr int NT = L * Shape<R1, R2>::RMAX;
+  constexpr int EIN = (L * N + NT - 1) / NT;   // input elements per thread
+  constexpr int EOUT = (L * M + NT - 1) / NT;  // output elements per thread
   const int p = blockIdx.y;
   const FieldDesc& fd = args.f[f0 + p];
   const int64_t row0 = (int64_t)blockIdx.x * L;
   const int64_t nrows = (int64_t)N * N;
-  for (int i = threadIdx.x; i < L * N; i += blockDim.x) {
-    const int line = i / N, z = i % N;
-    const int64_t r = row0 + line;
-    T2 v;
-    v.x = v.y = 0;
-    if (r < nrows) {
-      const int64_t gi = r * N + z;
-      v.x = dens<T>(fd.p[0], args.in, gi);
-      if (fd.p[1].a >= 0) v.y = dens<T>(fd.p[1], args.in, gi);
+  // the pair-density factors of the real and imaginary parts (null: factor absent)
+  const T* a0 = reinterpret_cast<const T*>(args.in[fd.p[0].a]);
+  const T* b0 = fd.p[0].b >= 0 ? reinterpret_cast<const T*>(args.in[fd.p[0].b]) : nullptr;
+  const T* a1 = fd.p[1].a >= 0 ? reinterpret_cast<const T*>(args.in[fd.p[1].a]) : nullptr;
+  const T* b1 = (a1 && fd.p[1].b >= 0) ? reinterpret_cast<const T*>(args.in[fd.p[1].b]) : nullptr;
+  // every load of this thread is issued before the first shared-memory store
+  T2 vin[EIN];
+#pragma unroll
+  for (int e = 0; e < EIN; ++e) {
+    const int i = threadIdx.x + e * NT;
+    const int64_t r = row0 + i / N;
+    vin[e].x = vin[e].y = 0;
+    if (i < L * N && r < nrows) {
+      const int64_t gi = r * N + i % N;
+      vin[e].x = a0[gi];
+      if (b0) vin[e].x *= b0[gi];
+      if (a1) {
+        vin[e].y = a1[gi];
+        if (b1) vin[e].y *= b1[gi];
+      }
     }
-    buf[z * LP + line] = v;
+  }
+#pragma unroll
+  for (int e = 0; e < EIN; ++e) {
+    const int i = threadIdx.x + e * NT;
+    if (i < L * N) buf[(i % N) * LP + i / N] = vin[e];
   }
   __syncthreads();
   const int t = threadIdx.x, line = t % L, q = t / L;
@@ -140,10 +160,12 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
     for (int k2 = 0; k2 < R2; ++k2) buf[(q + R1 * k2) * LP + line] = X[k2];
   __syncthreads();
   T2* dst = S1 + (int64_t)p * nrows * M;
-  for (int i = threadIdx.x; i < L * M; i += blockDim.x) {
+#pragma unroll
+  for (int e = 0; e < EOUT; ++e) {
+    const int i = threadIdx.x + e * NT;
     const int ln = i / M, kz = i % M;
     const int64_t r = row0 + ln;
-    if (r < nrows) dst[r * M + kz] = buf[kz * LP + ln];
+    if (i < L * M && r < nrows) dst[r * M + kz] = buf[kz * LP + ln];
   }
 }
 
@@ -177,14 +199,20 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   for (int p = 0; p < nfg; ++p) {
     const FieldDesc& fd = args.f[f0 + p];
     const T2* src = S1 + (int64_t)p * nrows * M;
+    constexpr int ESP = (L * M + NT - 1) / NT;
+    T2 vin[ESP];
+#pragma unroll
+    for (int e = 0; e < ESP; ++e) {
+      const int i = threadIdx.x + e * NT;
+      const int64_t r = row0 + i / M;
+      if (i < L * M && r < nrows) vin[e] = src[r * M + i % M];
+      else vin[e].x = vin[e].y = 0;
+    }
     __syncthreads();
-    for (int i = threadIdx.x; i < L * M; i += blockDim.x) {
-      const int ln = i / M, kz = i % M;
-      const int64_t r = row0 + ln;
-      T2 v;
-      if (r < nrows) v = src[r * M + kz];
-      else v.x = v.y = 0;
-      buf[kz * LP + ln] = v;
+#pragma unroll
+    for (int e = 0; e < ESP; ++e) {
+      const int i = threadIdx.x + e * NT;
+      if (i < L * M) buf[(i % M) * LP + i / M] = vin[e];
     }
     __syncthreads();
     T2 X[R2];
@@ -280,13 +308,22 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   const int64_t row0 = (int64_t)blockIdx.x * L;
   const int64_t nrows = (int64_t)N * N;
   const T2* src = S1 + (int64_t)p * nrows * M;
-  for (int i = threadIdx.x; i < L * M; i += blockDim.x) {
-    const int ln = i / M, kz = i % M;
-    const int64_t r = row0 + ln;
-    T2 v;
-    if (r < nrows) v = src[r * M + kz];
-    else v.x = v.y = 0;
-    buf[kz * LP + ln] = v;
+  constexpr int NT = L * Shape<R1, R2>::RMAX;
+  constexpr int ESP = (L * M + NT - 1) / NT;
+  {
+    T2 vin[ESP];
+#pragma unroll
+    for (int e = 0; e < ESP; ++e) {
+      const int i = threadIdx.x + e * NT;
+      const int64_t r = row0 + i / M;
+      if (i < L * M && r < nrows) vin[e] = src[r * M + i % M];
+      else vin[e].x = vin[e].y = 0;
+    }
+#pragma unroll
+    for (int e = 0; e < ESP; ++e) {
+      const int i = threadIdx.x + e * NT;
+      if (i < L * M) buf[(i % M) * LP + i / M] = vin[e];
+    }
   }
   __syncthreads();
   const int t = threadIdx.x, line = t % L, q = t / L;
@@ -311,10 +348,13 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   __syncthreads();
   T* jre = jbase + (int64_t)(2 * (f0 + p)) * jstride;
   T* jim = jre + jstride;
-  for (int i = threadIdx.x; i < L * N; i += blockDim.x) {
+  constexpr int EJ = (L * N + NT - 1) / NT;
+#pragma unroll
+  for (int e = 0; e < EJ; ++e) {
+    const int i = threadIdx.x + e * NT;
     const int ln = i / N, z = i % N;
     const int64_t r = row0 + ln;
-    if (r >= nrows) continue;
+    if (i >= L * N || r >= nrows) continue;
     const T2 J = buf[z * LP + ln];
     jre[r * N + z] = J.x;
     jim[r * N + z] = J.y;
