@@ -32,6 +32,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_DEFAULT, H_DEFAULT, N_OCC = 128, 0.25, 4
+# DRAM read + write of one x-pass launch (5 fields, 128^3) in the ncu capture
+# summarised in profiles/block_fock_apply_h2o128_f32_kernels.md
+FMI_TRAFFIC_128 = 345_278_976 + 275_794_432
 METRIC = "H2O 128^3 RHF block Fock-applies/s (mixed FP32/FP64 at |dE|<1uHa) and force time"
 UNIT = "Fock-applies/s"
 
@@ -336,8 +339,10 @@ def run_gato(args):
         "gpu_launches": int(launches),
         "roofline": {"kernel": "k_cols<float2, FMI> (x FFT, kernel multiply, inverse x FFT)", "bound": "hbm",
                      "achieved": bytes_x / tx_avg / 1e9, "peak": peak, "unit": "GB/s",
-                     "frac": bytes_x / tx_avg / 1e9 / peak, "traffic": None, "peak_kind": peak_kind,
-                     "algorithmic_bytes": bytes_x, "avg_launch_us": tx_avg * 1e6},
+                     "frac": bytes_x / tx_avg / 1e9 / peak,
+                     "traffic": FMI_TRAFFIC_128 if N == 128 else None, "peak_kind": peak_kind,
+                     "algorithmic_bytes": bytes_x, "avg_launch_us": tx_avg * 1e6,
+                     "limiter": "instruction issue (77% issue active, FMA pipe 55%, ncu)"},
         "roofline_stencil": {"bound": "hbm", "achieved": bytes_s / ts_avg / 1e9, "peak": peak, "unit": "GB/s",
                              "frac": bytes_s / ts_avg / 1e9 / peak, "avg_launch_us": ts_avg * 1e6},
         "cpu_baseline": cpu,
