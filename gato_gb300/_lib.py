@@ -73,6 +73,7 @@ _SIGS = {
     "gato_lanczos_finish": [i32, i64, vp, i32, i32, f64, vp, vp, vp, vp, vp, vp],
     "gato_hgh_local_grad": [i32, vp, i32, f64, i32, P_f64, P_f64, P_f64, P_f64, P_f64, vp],
     "gato_nonlocal_grad": [vp, vp, i32, P_f64, vp],
+    "gato_softened_coulomb_grad": [i32, vp, i32, f64, i32, P_f64, P_f64, f64, P_f64, vp],
 }
 
 

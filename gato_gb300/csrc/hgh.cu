@@ -122,6 +122,35 @@ __global__ void k_local_grad(const T* __restrict__ rho, int N, double L, double 
   }
 }
 
+// d/dR_k of int rho V_soft with V_soft = -Z_k / sqrt(|r - R_k|^2 + eps^2):
+// int rho(r) (-Z_k) (r - R_k) / (|r - R_k|^2 + eps^2)^{3/2} dV.
+template <typename T>
+__global__ void k_softened_grad(const T* __restrict__ rho, int N, double L, double h, AtomTable at,
+                                double eps, double* partials) {
+  __shared__ double sh[32];
+  const int64_t n3 = (int64_t)N * N * N;
+  const T e2 = (T)(eps * eps);
+  for (int k = 0; k < at.K; ++k) {
+    Acc<T> g[3];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n3;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      const int z = (int)(i % N), y = (int)((i / N) % N), x = (int)(i / ((int64_t)N * N));
+      const T dx = (T)(axis_coord(x, L, h) - at.x[k]);
+      const T dy = (T)(axis_coord(y, L, h) - at.y[k]);
+      const T dz = (T)(axis_coord(z, L, h) - at.z[k]);
+      const T u = dx * dx + dy * dy + dz * dz + e2;
+      const T w = -(T)at.Z[k] * rho[i] / (u * sqrt(u));
+      g[0].add_prod(w, dx);
+      g[1].add_prod(w, dy);
+      g[2].add_prod(w, dz);
+    }
+    for (int cc = 0; cc < 3; ++cc) {
+      const double v = block_sum(g[cc].value(), sh);
+      if (threadIdx.x == 0) partials[(k * 3 + cc) * gridDim.x + blockIdx.x] = v;
+    }
+  }
+}
+
 // ---- non-local projectors -------------------------------------------------------
 
 struct ProjParams {
@@ -439,6 +468,32 @@ extern "C" int gato_hgh_local_grad(int dtype, const void* rho, int N, double L, 
   double* res = part + 3 * K * nblk;
   if (dtype == GATO_F64) k_local_grad<double><<<nblk, 256, 0, s>>>((const double*)rho, N, L, h, at, part);
   else k_local_grad<float><<<nblk, 256, 0, s>>>((const float*)rho, N, L, h, at, part);
+  GATO_LAUNCH_TRY();
+  GATO_TRY(finalize_sums(part, 3 * K, nblk, h * h * h, res, s));
+  std::vector<double> g(3 * K);
+  GATO_CUDA_TRY(cudaMemcpyAsync(g.data(), res, 3 * K * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GATO_CUDA_TRY(cudaStreamSynchronize(s));
+  for (int i = 0; i < 3 * K; ++i) grad_host[i] += g[i];
+  return GATO_OK;
+}
+
+extern "C" int gato_softened_coulomb_grad(int dtype, const void* rho, int N, double L, int K,
+                                          const double* pos_host, const double* Z_host, double eps,
+                                          double* grad_host, void* stream) {
+  if (!rho || N < 1 || L <= 0 || K < 1 || !pos_host || !Z_host || !grad_host)
+    return fail(GATO_EBADARG, "gato_softened_coulomb_grad: bad arguments");
+  AtomTable at;
+  GATO_TRY(make_atoms(at, K, pos_host, Z_host, nullptr, nullptr));
+  cudaStream_t s = as_stream(stream);
+  const double h = L / N;
+  const int nblk = kRedBlocks;
+  double* part = (double*)stream_scratch(s, (size_t)(3 * K * nblk + 3 * K) * sizeof(double));
+  if (!part) return fail(GATO_ENOMEM, "scratch");
+  double* res = part + 3 * K * nblk;
+  if (dtype == GATO_F64)
+    k_softened_grad<double><<<nblk, 256, 0, s>>>((const double*)rho, N, L, h, at, eps, part);
+  else
+    k_softened_grad<float><<<nblk, 256, 0, s>>>((const float*)rho, N, L, h, at, eps, part);
   GATO_LAUNCH_TRY();
   GATO_TRY(finalize_sums(part, 3 * K, nblk, h * h * h, res, s));
   std::vector<double> g(3 * K);

@@ -37,6 +37,26 @@ def multi_center_softened_coulomb(nuclei: Nuclei, grid: Grid3D, epsilon: float |
     return _softened(grid, _t(nuclei.positions).detach(), _t(nuclei.charges).detach(), epsilon, dtype)
 
 
+def multi_center_softened_coulomb_grad(nuclei: Nuclei, grid: Grid3D, rho, epsilon: float | None = None
+                                       ) -> torch.Tensor:
+    """d/dR of int rho V_ext dV for the multi-centre softened Coulomb V_ext, (K, 3) float64 host.
+
+    The force term the reference obtains with jax.grad through
+    multi_center_softened_coulomb (physics/h2.py:109-135).
+    """
+    from .grid import as_field
+    if epsilon is None:
+        epsilon = grid.h / 2
+    rho = as_field(rho)
+    pos = [float(v) for v in _t(nuclei.positions).detach().to(torch.float64).reshape(-1)]
+    Z = [float(v) for v in _t(nuclei.charges).detach().to(torch.float64).reshape(-1)]
+    g = (C.c_double * (3 * len(Z)))()
+    _lib.call("gato_softened_coulomb_grad", _lib.dtype_code(rho), C.c_void_p(rho.data_ptr()), grid.N,
+              float(grid.L), len(Z), _lib.dbl_array(pos), _lib.dbl_array(Z), float(epsilon), g,
+              C.c_void_p(_lib.stream()))
+    return torch.tensor(list(g), dtype=torch.float64).reshape(len(Z), 3)
+
+
 def harmonic_oscillator(grid: Grid3D, omega: float = 1.0) -> torch.Tensor:
     """1/2 omega^2 r^2 (potentials.py:64-69); a test fixture."""
     X, Y, Z = grid.coords()

@@ -210,6 +210,13 @@ int gato_hgh_local_grad(int dtype, const void* rho, int N, double L, int K, cons
                         const double* Zion_host, const double* rloc_host, const double* c_host,
                         double* grad_host, void* stream);
 int gato_nonlocal_grad(gato_nonlocal_t nl, const void* orbitals, int n, double* grad_host, void* stream);
+/* grad_host (K*3) += d/dR of int rho V_ext for the multi-centre softened
+ * Coulomb V_ext = -sum_k Z_k / sqrt(|r - R_k|^2 + eps^2) (potentials.py:39-61);
+ * the H2 driver's force, which the reference takes with jax.grad
+ * (physics/h2.py:109-135).                                                 */
+int gato_softened_coulomb_grad(int dtype, const void* rho, int N, double L, int K,
+                               const double* pos_host, const double* Z_host, double eps,
+                               double* grad_host, void* stream);
 
 #ifdef __cplusplus
 }

@@ -259,6 +259,21 @@ def multi_center_softened_coulomb(nuclei, grid, epsilon=None):              # po
     return V
 
 
+def multi_center_softened_coulomb_grad(nuclei, grid, rho, epsilon=None):
+    """d/dR_k of int rho V_ext dV for V_ext = multi_center_softened_coulomb: the force term
+    physics/h2.py:109-135 takes with jax.grad; analytic: -Z_k (r - R_k) / (|r - R_k|^2 + eps^2)^{3/2}."""
+    if epsilon is None:
+        epsilon = grid.h / 2
+    X, Y, Zc = grid.coords()
+    g = np.zeros((len(nuclei.charges), 3))
+    for k, (R, Zk) in enumerate(zip(nuclei.positions, nuclei.charges)):
+        d = (X - R[0], Y - R[1], Zc - R[2])
+        w = -Zk * rho / (d[0] ** 2 + d[1] ** 2 + d[2] ** 2 + epsilon * epsilon) ** 1.5
+        for c in range(3):
+            g[k, c] = np.sum(w * d[c]) * grid.dV
+    return g
+
+
 def harmonic_oscillator(grid, omega=1.0):  # potentials.py:64-69 (test fixture)
     X, Y, Z = grid.coords()
     return 0.5 * omega * omega * (X * X + Y * Y + Z * Z)

@@ -345,3 +345,22 @@ def test_adam_matches_published_update():
     g = np.array([[0.3, -2.0, 1e-3]])
     u = opt.update(g)
     assert np.allclose(u, -0.02 * g / (np.abs(g) + 1e-8), rtol=1e-12)
+
+
+def test_softened_coulomb_grad_matches_finite_difference():
+    """The analytic d/dR int rho V_ext of the H2 force path against a central difference."""
+    g = o.Grid3D(24, 8.0)
+    X, Y, Z = g.coords()
+    rho = np.exp(-0.6 * (X * X + Y * Y + (Z - 0.2) ** 2))
+    pos = np.array([[0.0, 0.1, -0.7], [0.05, 0.0, 0.7]])
+    nuc = o.Nuclei(pos, np.array([1.0, 1.0]))
+    ga = o.multi_center_softened_coulomb_grad(nuc, g, rho, 0.3)
+    d = 1e-4
+    for k in range(2):
+        for c in range(3):
+            pp, pm = pos.copy(), pos.copy()
+            pp[k, c] += d
+            pm[k, c] -= d
+            ep = np.sum(rho * o.multi_center_softened_coulomb(o.Nuclei(pp, nuc.charges), g, 0.3)) * g.dV
+            em = np.sum(rho * o.multi_center_softened_coulomb(o.Nuclei(pm, nuc.charges), g, 0.3)) * g.dV
+            assert abs(ga[k, c] - (ep - em) / (2 * d)) < 1e-7
