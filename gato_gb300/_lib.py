@@ -59,6 +59,9 @@ _SIGS = {
     "gato_axpby": [i32, vp, vp, vp, i64, f64, f64, vp],
     "gato_field_sum": [i32, vp, i32, i64, vp, vp],
     "gato_convert": [i32, vp, i32, vp, i64, vp],
+    "gato_dot_weighted": [i32, vp, vp, vp, i64, f64, vp, vp],
+    "gato_imag_time": [i32, vp, vp, i32, f64, i32, i32, f64, i32, i32, vp, vp],
+    "gato_radial_density": [i32, vp, vp, i32, f64, P_f64, i32, vp, vp],
     "gato_op_create": [i32, i32, f64, i32, i32, C.POINTER(vp)],
     "gato_op_destroy": [vp],
     "gato_op_set_potential": [vp, vp],

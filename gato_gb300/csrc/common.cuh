@@ -42,8 +42,14 @@ int* device_error_word();
 // The first call on a stream may allocate; later calls of the same or
 // smaller size do not. Slot 0 serves leaf reductions; a driver that calls
 // leaf operations while holding scratch uses its own slot.
-enum ScratchSlot { kSlotLeaf = 0, kSlotLanczos = 1, kSlotCount = 2 };
+enum ScratchSlot { kSlotLeaf = 0, kSlotLanczos = 1, kSlotImagTime = 2, kSlotCount = 3 };
 void* stream_scratch(cudaStream_t s, size_t bytes, int slot = kSlotLeaf);
+// Free every scratch slot of stream s (synchronises s first): for private
+// streams that are about to be destroyed.
+void release_stream_scratch(cudaStream_t s);
+// sum_i a_i b_i * scale into out[0] (device), FP64 / float-float accumulation.
+int dot_impl(int dtype, const void* a, const void* b, int64_t n, double scale, double* out,
+             cudaStream_t s);
 
 // Elementwise launch geometry: a grid-stride loop over n items.
 inline unsigned grid_for(int64_t n, int threads, int max_blocks = 152 * 16) {

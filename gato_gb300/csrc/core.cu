@@ -65,6 +65,19 @@ void* stream_scratch(cudaStream_t s, size_t bytes, int slot) {
   return p;
 }
 
+void release_stream_scratch(cudaStream_t s) {
+  cudaStreamSynchronize(s);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (int slot = 0; slot < kSlotCount; ++slot) {
+    auto it = g_scratch.find({{dev, slot}, s});
+    if (it == g_scratch.end()) continue;
+    if (it->second.first) cudaFree(it->second.first);
+    g_scratch.erase(it);
+  }
+}
+
 __global__ void k_finalize_sums(const double* partials, int nparts, double scale, double* out) {
   __shared__ double sh[32];
   const double* p = partials + (size_t)blockIdx.x * nparts;
@@ -124,6 +137,19 @@ __global__ void k_dot_partials(const T* __restrict__ a, const T* __restrict__ b,
     if (b) acc.add_prod(a[i], b[i]);
     else acc.add(a[i]);
   }
+  double v = block_sum(acc.value(), sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = v;
+}
+
+// sum_i a_i w_i b_i: the <psi|V|psi> of observables.py:26-30
+template <typename T>
+__global__ void k_wdot_partials(const T* __restrict__ a, const T* __restrict__ w, const T* __restrict__ b,
+                                int64_t n, double* partials) {
+  __shared__ double sh[32];
+  Acc<T> acc;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    acc.add_prod(a[i] * w[i], b[i]);
   double v = block_sum(acc.value(), sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = v;
 }
@@ -202,6 +228,24 @@ extern "C" int gato_dot(int dtype, const void* a, const void* b, int64_t n, doub
                         double* out_dev, void* stream) {
   if (dtype != GATO_F64 && dtype != GATO_F32) return fail(GATO_EBADARG, "bad dtype %d", dtype);
   return dot_impl(dtype, a, b, n, scale, out_dev, as_stream(stream));
+}
+
+extern "C" int gato_dot_weighted(int dtype, const void* a, const void* w, const void* b, int64_t n,
+                                 double scale, double* out_dev, void* stream) {
+  if (!a || !w || !b || !out_dev || n <= 0) return fail(GATO_EBADARG, "gato_dot_weighted: bad arguments");
+  if (dtype != GATO_F64 && dtype != GATO_F32) return fail(GATO_EBADARG, "bad dtype %d", dtype);
+  cudaStream_t s = as_stream(stream);
+  double* part = (double*)stream_scratch(s, kRedBlocks * sizeof(double));
+  if (!part) return fail(GATO_ENOMEM, "gato_dot_weighted: scratch allocation failed");
+  const int nb = (int)grid_for(n, kRedThreads, kRedBlocks);
+  if (dtype == GATO_F64)
+    k_wdot_partials<double><<<nb, kRedThreads, 0, s>>>((const double*)a, (const double*)w, (const double*)b,
+                                                        n, part);
+  else
+    k_wdot_partials<float><<<nb, kRedThreads, 0, s>>>((const float*)a, (const float*)w, (const float*)b, n,
+                                                       part);
+  GATO_LAUNCH_TRY();
+  return finalize_sums(part, 1, nb, scale, out_dev, s);
 }
 
 extern "C" int gato_normalize(int dtype, void* a, int64_t n, const double* nsq, void* stream) {

@@ -16,6 +16,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 
 #include "common.cuh"
@@ -280,7 +281,16 @@ int launch_tma_mode(const CUtensorMap& tm, const CUtensorMap& vm, void* out, int
                     cudaStream_t s) {
   using G = TmaGeom<T, R>;
   auto kern = k_stencil_tma<T, R, HAS_V, STORE, DOT>;
-  GATO_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM));
+  // opt in to the large shared-memory carve-out once per device (the launch
+  // itself then issues only stream work, so it can be graph-captured)
+  static std::atomic<unsigned> attr_done{0};
+  int dev = 0;
+  GATO_CUDA_TRY(cudaGetDevice(&dev));
+  const unsigned bit = 1u << (dev & 31);
+  if (!(attr_done.load() & bit)) {
+    GATO_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM));
+    attr_done.fetch_or(bit);
+  }
   const int tiles_z = (nz + kBZ - 1) / kBZ, tiles_y = (ny + kBY - 1) / kBY;
   const int tiles = tiles_z * tiles_y;
   // Split x into chunks so the grid is one full resident wave where the

@@ -150,6 +150,10 @@ int gato_axpby(int dtype, const void* x, const void* y, void* out, int64_t npts,
 /* dst = (dst dtype) src, n elements: the precision changes between the FP32
  * Fock applies and the FP64 density / Hartree / energy of the mixed SCF.    */
 int gato_convert(int src_dtype, const void* src, int dst_dtype, void* dst, int64_t n, void* stream);
+/* out_dev[0] = scale * sum_i a_i w_i b_i: <psi|V|psi> of potential_energy
+ * (observables.py:26-30).                                                  */
+int gato_dot_weighted(int dtype, const void* a, const void* w, const void* b, int64_t n, double scale,
+                      double* out_dev, void* stream);
 /* out = sum_k fields[k]: the Lanczos seed sum(orbitals, axis=-1) (scf.py:417). */
 int gato_field_sum(int dtype, const void* fields, int nf, int64_t npts, void* out, void* stream);
 /* out += coef * K psi, K psi = sum_j phi_j J[phi_j psi]: scf.py:66-85.     */
@@ -200,6 +204,20 @@ int gato_lanczos_step(int dtype, int64_t n, double dV, void* krylov, int j, int 
 int gato_lanczos_finish(int dtype, int64_t n, const void* krylov, int m, int K, double tol,
                         const double* alphas_dev, const double* betas_dev, double* evals_dev,
                         void* evecs, int* flag_dev, void* stream);
+
+/* ---- solvers/imag_time.py:29-65, observables.py:41-59 ----------------------
+ * gato_imag_time: psi (in/out, N^3) <- n_steps Euler steps of
+ * psi <- (psi - dt H psi) / |psi - dt H psi| with H = -1/2 Laplacian + V
+ * (V null: no potential), after normalising psi. energies_dev receives the
+ * Rayleigh quotient after every step i with i % log_every == 0 or
+ * i == n_steps - 1, in order. The step is replayed as a CUDA graph.
+ * gato_radial_density: hist_dev[k] = sum over grid points with radius in
+ * [edges[k], edges[k+1]) (last bin closed) of (re^2 + im^2) dV, im optional;
+ * edges_host holds n_bins + 1 increasing radii (numpy.histogram binning).  */
+int gato_imag_time(int dtype, void* psi, const void* V, int N, double h, int order, int boundary, double dt,
+                   int n_steps, int log_every, double* energies_dev, void* stream);
+int gato_radial_density(int dtype, const void* re, const void* im, int N, double L, const double* edges_host,
+                        int n_bins, double* hist_dev, void* stream);
 
 /* ---- physics/water.py: Hellmann-Feynman forces -----------------------------
  * grad_host (K*3, host doubles, ACCUMULATED into) += d/dR of the R-dependent

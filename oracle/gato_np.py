@@ -622,6 +622,50 @@ def imaginary_time(H, psi0, dt=None, n_steps=2000):
     return psi, float(H.rayleigh(psi))
 
 
+def imaginary_time_logged(H, psi0, dt=None, n_steps=2000, log_every=50):
+    """solvers/imag_time.py:29-65 with its log: (psi, steps, Rayleigh quotients)."""
+    grid = H.grid
+    if dt is None:
+        dt = grid.h ** 2 / 10.0
+    psi = psi0 / np.sqrt(norm_sq(psi0, grid))
+    steps, energies = [], []
+    for i in range(n_steps):
+        psi_new = psi - dt * H.apply(psi)
+        psi = psi_new / np.sqrt(norm_sq(psi_new, grid))
+        if i % log_every == 0 or i == n_steps - 1:
+            steps.append(i)
+            energies.append(float(H.rayleigh(psi)))
+    return psi, steps, energies
+
+
+# ---------------------------------------------------------------------------
+# observables.py
+# ---------------------------------------------------------------------------
+
+def kinetic_energy(psi, grid, boundary="dirichlet", order=2):     # observables.py:16-21
+    return inner_product(psi, kinetic(psi, grid.h, boundary, order), grid).real / norm_sq(psi, grid).real
+
+
+def potential_energy(psi, V, grid):                               # observables.py:24-28
+    return inner_product(psi, V * psi, grid).real / norm_sq(psi, grid).real
+
+
+def virial_ratio(psi, V, grid, boundary="dirichlet", order=2):    # observables.py:31-44
+    return 2 * kinetic_energy(psi, grid, boundary, order) / abs(potential_energy(psi, V, grid))
+
+
+def radial_density(psi, grid, n_bins=100, r_max=None):            # observables.py:47-59
+    r = grid.radial().reshape(-1)
+    density = (np.abs(psi) ** 2 * grid.dV).reshape(-1)
+    if r_max is None:
+        r_max = float(grid.L / 2)
+    bins = np.linspace(0.0, r_max, n_bins + 1)
+    centers = 0.5 * (bins[1:] + bins[:-1])
+    widths = bins[1:] - bins[:-1]
+    hist, _ = np.histogram(r, bins=bins, weights=density)
+    return centers, hist / widths
+
+
 # ---------------------------------------------------------------------------
 # scf.py
 # ---------------------------------------------------------------------------
