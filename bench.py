@@ -374,6 +374,26 @@ def run_workload(args):
 
     from gato_gb300.grid import Grid3D
     out = {"workload": args.workload}
+    if args.workload == "c5":
+        # 48 seeded systems (H2 / LiH / HCl / H2O, 64^3..160^3, h 0.2..0.3), mixed precision,
+        # concurrent streams vs one stream, FP64 continuation checks on the grids <= 96^3
+        from gato_gb300.batch import draw_systems, fp64_check, solve_batch, summarize
+        specs = draw_systems(48, seed=0)
+        res, wall = solve_batch(specs, precision="mixed", streams=args.streams, max_iters=80, tol=1e-8)
+        out["concurrent"] = summarize(res, wall)
+        out["concurrent"]["streams"] = args.streams
+        if args.c5_sequential:
+            _, wall1 = solve_batch(specs, precision="mixed", streams=1, max_iters=80, tol=1e-8)
+            out["sequential_wall_s"] = wall1
+            out["concurrency_speedup"] = wall1 / wall
+        checks = [fp64_check(r) for r in res if r.spec.N <= 96]
+        both = [c for c in checks if c["fp64_converged"] and c["mixed_converged"]]
+        out["fp64_checks"] = {"systems": len(checks), "both_converged": len(both),
+                              "max_abs_dE_converged": max((c["abs_dE"] for c in both), default=None),
+                              "max_abs_dF_same_orbitals": max(c["max_abs_dF"] for c in checks),
+                              "per_system": checks}
+        print(json.dumps(out), flush=True)
+        return
     if args.workload == "c1":
         # hydrogen 64^3, L = 20, 7-point Laplacian, softened Coulomb a = 0.1, Lanczos m = 80, K = 1
         from gato_gb300.hamiltonian import Hamiltonian
@@ -514,7 +534,9 @@ def run_profile(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default=None, choices=["c1", "c2", "c3", "c4"],
+    ap.add_argument("--streams", type=int, default=8, help="concurrent streams of the c5 batch")
+    ap.add_argument("--c5-sequential", type=int, default=1, help="also time the c5 batch on one stream")
+    ap.add_argument("--workload", default=None, choices=["c1", "c2", "c3", "c4", "c5"],
                     help="run a configuration workload instead of the headline metric")
     ap.add_argument("--fp64-iters", type=int, default=3)
     ap.add_argument("--geom-steps", type=int, default=60)

@@ -11,6 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import threading
 from collections import OrderedDict
 from dataclasses import dataclass
 
@@ -165,12 +166,16 @@ class HGHNonlocal:
         return torch.tensor(list(g), dtype=torch.float64).reshape(K, 3)
 
 
-_NL_CACHE: "OrderedDict[tuple, HGHNonlocal]" = OrderedDict()
+# Per-thread, like the Poisson plans: an operator's projection scratch serves one stream at a time.
+_NL_TLS = threading.local()
 
 
 def nonlocal_for(nuclei: Nuclei, elements, grid: Grid3D, dtype=torch.float64) -> HGHNonlocal:
     key = (tuple(_pos_list(nuclei)), tuple(p.symbol for p in elements), tuple(id(p) for p in elements),
            grid.N, float(grid.L), dtype)
+    _NL_CACHE = getattr(_NL_TLS, "cache", None)
+    if _NL_CACHE is None:
+        _NL_CACHE = _NL_TLS.cache = OrderedDict()
     nl = _NL_CACHE.get(key)
     if nl is None:
         nl = HGHNonlocal(nuclei, elements, grid, dtype)

@@ -8,6 +8,7 @@ every call).
 from __future__ import annotations
 
 import ctypes as C
+import threading
 from collections import OrderedDict
 
 import torch
@@ -53,10 +54,21 @@ class PoissonPlan:
         return out
 
 
-_PLANS: "OrderedDict[tuple, PoissonPlan]" = OrderedDict()
+# Plans own spectral work buffers, which one stream at a time may use: the
+# cache is per thread, so threads driving their own streams never share one.
+_TLS = threading.local()
+
+
+def _plans() -> "OrderedDict[tuple, PoissonPlan]":
+    d = getattr(_TLS, "plans", None)
+    if d is None:
+        d = _TLS.plans = OrderedDict()
+    return d
 
 
 def get_plan(N: int, h: float, eps: float, dtype=torch.float64, max_fields: int = 6) -> PoissonPlan:
+    """The calling thread's cached plan for (N, h, eps, dtype), built if absent (3 kept per thread)."""
+    _PLANS = _plans()
     key = (N, float(h), float(eps), dtype)
     p = _PLANS.get(key)
     if p is None or p.max_fields < max_fields:

@@ -117,3 +117,16 @@ def test_lookup_and_tables():
     with pytest.raises(KeyError):
         lookup("Xx")
     assert total_valence_charge((lookup("O"), lookup("H"), lookup("H"))) == 8.0
+
+
+def test_grid_convergence_power_law_fit():
+    """The scan fit of benchmarks/grid_convergence.py recovers a known law; < 3 points -> nan."""
+    import math
+
+    import numpy as np
+
+    from gato_gb300.benchmarks.grid_convergence import fit_power_law
+    h = np.array([0.35, 0.3, 0.25, 0.2, 0.15])
+    e_inf, C, p, rms = fit_power_law(h, -17.3 + 2.0 * h ** 3.5)
+    assert abs(e_inf + 17.3) < 1e-9 and abs(C - 2.0) < 1e-7 and abs(p - 3.5) < 1e-9 and rms < 1e-10
+    assert all(math.isnan(v) for v in fit_power_law([0.2, 0.1], [1.0, 2.0]))

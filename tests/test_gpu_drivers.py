@@ -204,3 +204,26 @@ def test_helium_matches_oracle_and_virial():
     assert abs(he.energy - ref.energy) < 1e-8, (he.energy, ref.energy)
     assert abs(he.kinetic + he.potential + he.hartree + he.exchange - he.energy) < 1e-10
     assert 0.8 < he.virial_ratio < 1.2
+
+
+@pytest.mark.parametrize("mode", ["energy", "box"])
+def test_grid_convergence_sweeps(mode, tmp_path):
+    import json
+
+    from gato_gb300.benchmarks.grid_convergence import main
+    out_file = tmp_path / "conv.json"
+    if mode == "energy":
+        out = main(["--molecule", "water", "--mode", "energy", "--N", "24", "32", "40", "--L", "10",
+                    "--precision", "mixed", "--scf-iters", "60", "--json", str(out_file)])
+    else:
+        out = main(["--molecule", "hcl", "--mode", "box", "--box-L", "8", "9", "10", "--target-h", "0.25",
+                    "--scf-iters", "60", "--json", str(out_file)])
+        assert out["h_drift"] is False and [r["N"] for r in out["rows"]] == [32, 36, 40]
+    assert all(r["converged"] for r in out["rows"])
+    assert out["fit"] is not None and math_isfinite(out["fit"]["extrapolated"])
+    assert json.loads(out_file.read_text())["rows"][0]["N"] == out["rows"][0]["N"]
+
+
+def math_isfinite(x):
+    import math
+    return math.isfinite(x)
