@@ -383,9 +383,13 @@ def run_workload(args):
         out["concurrent"] = summarize(res, wall)
         out["concurrent"]["streams"] = args.streams
         if args.c5_sequential:
-            _, wall1 = solve_batch(specs, precision="mixed", streams=1, max_iters=80, tol=1e-8)
+            res1, wall1 = solve_batch(specs, precision="mixed", streams=1, max_iters=80, tol=1e-8)
             out["sequential_wall_s"] = wall1
             out["concurrency_speedup"] = wall1 / wall
+            # same kernels on the same inputs: the two runs must agree bit for bit
+            out["bitwise_mismatches_vs_sequential"] = [
+                a.spec.name for a, b in zip(res, res1)
+                if a.point.energy != b.point.energy or not torch.equal(a.forces, b.forces)]
         checks = [fp64_check(r) for r in res if r.spec.N <= 96]
         both = [c for c in checks if c["fp64_converged"] and c["mixed_converged"]]
         out["fp64_checks"] = {"systems": len(checks), "both_converged": len(both),

@@ -113,6 +113,7 @@ def solve_batch(specs, *, precision: str = "mixed", streams: int = 8, max_iters:
         work.put(i)
     results: list = [None] * len(specs)
     errors: list = []
+    seq = [0] * max(1, streams)   # position of each system in its worker's sequence
 
     def worker(k: int):
         torch.cuda.set_device(dev)
@@ -131,7 +132,9 @@ def solve_batch(specs, *, precision: str = "mixed", streams: int = 8, max_iters:
                 except BaseException as e:   # surfaced to the caller after the pool stops
                     errors.append(e)
                     return
-                results[i] = SystemResult(specs[i], p, F, time.perf_counter() - t0, k)
+                results[i] = SystemResult(specs[i], p, F, time.perf_counter() - t0, k,
+                                          {"worker_seq": seq[k]})
+                seq[k] += 1
 
     torch.cuda.synchronize()
     t0 = time.perf_counter()

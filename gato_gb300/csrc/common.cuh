@@ -1,5 +1,6 @@
 // Shared device/host utilities of libgato_cuda (sm_103a only).
 #pragma once
+#include <initializer_list>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
@@ -47,6 +48,12 @@ void* stream_scratch(cudaStream_t s, size_t bytes, int slot = kSlotLeaf);
 // Free every scratch slot of stream s (synchronises s first): for private
 // streams that are about to be destroyed.
 void release_stream_scratch(cudaStream_t s);
+// cudaFree of device memory whose last users may still be queued on some
+// stream: waits for the device first, since cudaFree itself only "may"
+// synchronise, and memory it returned early could be handed to another
+// thread's allocation while those kernels still write it. Null entries are
+// skipped; nothing is waited for when all are null.
+void free_after_pending(std::initializer_list<void*> ptrs);
 // sum_i a_i b_i * scale into out[0] (device), FP64 / float-float accumulation.
 int dot_impl(int dtype, const void* a, const void* b, int64_t n, double scale, double* out,
              cudaStream_t s);

@@ -54,7 +54,11 @@ void* stream_scratch(cudaStream_t s, size_t bytes, int slot) {
   std::lock_guard<std::mutex> lk(g_mu);
   auto& e = g_scratch[{{dev, slot}, s}];
   if (e.second >= bytes) return e.first;
-  if (e.first) cudaFree(e.first);  // cudaFree synchronises with in-flight work
+  if (e.first) {
+    // the old buffer's users are this stream's queued kernels: let them finish first
+    cudaStreamSynchronize(s);
+    cudaFree(e.first);
+  }
   size_t sz = bytes < (1u << 20) ? (1u << 20) : bytes;
   void* p = nullptr;
   if (cudaMalloc(&p, sz) != cudaSuccess) {
@@ -63,6 +67,15 @@ void* stream_scratch(cudaStream_t s, size_t bytes, int slot) {
   }
   e = {p, sz};
   return p;
+}
+
+void free_after_pending(std::initializer_list<void*> ptrs) {
+  bool any = false;
+  for (void* p : ptrs) any = any || p != nullptr;
+  if (!any) return;
+  cudaDeviceSynchronize();
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
 }
 
 void release_stream_scratch(cudaStream_t s) {

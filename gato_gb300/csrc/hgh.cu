@@ -647,9 +647,8 @@ extern "C" int gato_nonlocal_create(int dtype, int N, double L, int K, const dou
 extern "C" int gato_nonlocal_destroy(gato_nonlocal_t w) {
   if (!w) return GATO_OK;
   Nonlocal& nl = w->n;
-  void* ps[] = {nl.vals, nl.d_q_atom, nl.d_q_off, nl.d_q_block, nl.d_q_n, nl.d_q_i,
-                nl.d_q_h, nl.d_box, nl.ov, nl.coef, nl.dov, nl.part};
-  for (void* p : ps) cudaFree(p);
+  free_after_pending({nl.vals, nl.d_q_atom, nl.d_q_off, nl.d_q_block, nl.d_q_n, nl.d_q_i, nl.d_q_h, nl.d_box,
+                      nl.ov, nl.coef, nl.dov, nl.part});
   delete w;
   return GATO_OK;
 }

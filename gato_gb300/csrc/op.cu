@@ -129,9 +129,7 @@ extern "C" int gato_op_create(int dtype, int N, double h, int order, int boundar
 
 extern "C" int gato_op_destroy(gato_op_t op) {
   if (!op) return GATO_OK;
-  cudaFree(op->dscratch);
-  cudaFree(op->rho);
-  cudaFree(op->jbuf);
+  free_after_pending({op->dscratch, op->rho, op->jbuf});
   delete op;
   return GATO_OK;
 }
@@ -182,7 +180,7 @@ extern "C" int gato_op_apply_block(gato_op_t op, void* out, void* stream) {
     // pair potentials to J fields, then one elementwise pass: out_i -= sum_j phi_j J_ij
     const size_t need = (size_t)2 * a.nf * op_n3(*op) * op_esize(*op);
     if (op->jbuf_bytes < need) {
-      cudaFree(op->jbuf);
+      free_after_pending({op->jbuf});
       op->jbuf = nullptr;
       op->jbuf_bytes = 0;
       GATO_CUDA_TRY(cudaMalloc(&op->jbuf, need));

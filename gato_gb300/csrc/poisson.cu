@@ -436,11 +436,7 @@ static int plan_create(int dtype, int N, double h, double eps, int max_fields, P
 }
 
 static void plan_free(PoissonPlan& pl) {
-  cudaFree(pl.ghat);
-  cudaFree(pl.tw);
-  cudaFree(pl.S1);
-  cudaFree(pl.S2);
-  cudaFree(pl.partials);
+  free_after_pending({pl.ghat, pl.tw, pl.S1, pl.S2, pl.partials});
   pl = PoissonPlan{};
 }
 

@@ -9,10 +9,29 @@ namespace fast {
 
 using namespace fft2;
 
-template <typename T2>
-__device__ __forceinline__ void load_tw(T2* tws, const T2* tw, int M) {
-  for (int i = threadIdx.x; i < M; i += blockDim.x) tws[i] = tw[i];
-}
+
+// The M-entry twiddle table split into a register prefetch at kernel entry
+// and a shared-memory store placed after the kernel's own field loads are
+// issued, so the two global latencies overlap instead of adding up.
+template <typename T2, int M, int NT>
+struct TwPrefetch {
+  static constexpr int K = (M + NT - 1) / NT;
+  T2 v[K];
+  __device__ __forceinline__ explicit TwPrefetch(const T2* tw) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int i = threadIdx.x + k * NT;
+      if (i < M) v[k] = tw[i];
+    }
+  }
+  __device__ __forceinline__ void store(T2* tws) const {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int i = threadIdx.x + k * NT;
+      if (i < M) tws[i] = v[k];
+    }
+  }
+};
 
 // Strided-line passes (y forward, x forward * kernel * x inverse, y inverse).
 // FULL: every CTA has L real columns (ncols % L == 0), so no per-access guard.
@@ -25,7 +44,7 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   extern __shared__ __align__(16) unsigned char smraw[];
   T2* buf = reinterpret_cast<T2*>(smraw);
   T2* tws = buf + M * LP;
-  load_tw(tws, tw, M);
+  const TwPrefetch<T2, M, L * Shape<R1, R2>::RMAX> twp(tw);
   const int outer = blockIdx.x, col0 = blockIdx.y * L, f = blockIdx.z;
   const int t = threadIdx.x;
   const int line = t % L, q = t / L;   // q: n2 in stages 1/B, k1 in stages 2/A
@@ -45,6 +64,7 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
         return v;
       });
     }
+    twp.store(tws);
     __syncthreads();
     if (q < R1) fwd_stage2<T2, R1, R2>(buf, LP, line, q, tws, X);
   } else {
@@ -57,6 +77,7 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
         else X[k2].x = X[k2].y = 0;
       }
     }
+    twp.store(tws);   // first read in inv_stageA, behind the barrier below
   }
   if (MODE == COL_FWD) {
     if (q < R1 && live) {
@@ -104,8 +125,8 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   extern __shared__ __align__(16) unsigned char smraw[];
   T2* buf = reinterpret_cast<T2*>(smraw);
   T2* tws = buf + M * LP;
-  load_tw(tws, tw, M);
   constexpr int NT = L * Shape<R1, R2>::RMAX;
+  const TwPrefetch<T2, M, NT> twp(tw);
   constexpr int EIN = (L * N + NT - 1) / NT;   // input elements per thread
   constexpr int EOUT = (L * M + NT - 1) / NT;  // output elements per thread
   const int p = blockIdx.y;
@@ -134,6 +155,7 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
       }
     }
   }
+  twp.store(tws);
 #pragma unroll
   for (int e = 0; e < EIN; ++e) {
     const int i = threadIdx.x + e * NT;
@@ -186,7 +208,7 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   __shared__ double sh[32];
   T2* buf = reinterpret_cast<T2*>(smraw);
   T2* tws = buf + M * LP;
-  load_tw(tws, tw, M);
+  const TwPrefetch<T2, M, NT> twp(tw);
   const int64_t row0 = (int64_t)blockIdx.x * L;
   const int64_t nrows = (int64_t)N * N;
   T acc[ENERGY ? 1 : NO][EPT];
@@ -199,20 +221,30 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   for (int p = 0; p < nfg; ++p) {
     const FieldDesc& fd = args.f[f0 + p];
     const T2* src = S1 + (int64_t)p * nrows * M;
+    // loads in batches of at most 8 elements per thread (the accumulators
+    // already hold NO x EPT registers); the first batch is in flight across
+    // the barrier that frees buf
     constexpr int ESP = (L * M + NT - 1) / NT;
-    T2 vin[ESP];
+    constexpr int CH = ESP < 8 ? ESP : 8;
 #pragma unroll
-    for (int e = 0; e < ESP; ++e) {
-      const int i = threadIdx.x + e * NT;
-      const int64_t r = row0 + i / M;
-      if (i < L * M && r < nrows) vin[e] = src[r * M + i % M];
-      else vin[e].x = vin[e].y = 0;
-    }
-    __syncthreads();
+    for (int c = 0; c < ESP; c += CH) {
+      T2 vin[CH];
 #pragma unroll
-    for (int e = 0; e < ESP; ++e) {
-      const int i = threadIdx.x + e * NT;
-      if (i < L * M) buf[(i % M) * LP + i / M] = vin[e];
+      for (int e = 0; e < CH; ++e) {
+        const int i = threadIdx.x + (c + e) * NT;
+        const int64_t r = row0 + i / M;
+        if (c + e < ESP && i < L * M && r < nrows) vin[e] = src[r * M + i % M];
+        else vin[e].x = vin[e].y = 0;
+      }
+      if (c == 0) {
+        if (p == 0) twp.store(tws);
+        __syncthreads();
+      }
+#pragma unroll
+      for (int e = 0; e < CH; ++e) {
+        const int i = threadIdx.x + (c + e) * NT;
+        if (c + e < ESP && i < L * M) buf[(i % M) * LP + i / M] = vin[e];
+      }
     }
     __syncthreads();
     T2 X[R2];
@@ -303,12 +335,12 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   extern __shared__ __align__(16) unsigned char smraw[];
   T2* buf = reinterpret_cast<T2*>(smraw);
   T2* tws = buf + M * LP;
-  load_tw(tws, tw, M);
+  constexpr int NT = L * Shape<R1, R2>::RMAX;
+  const TwPrefetch<T2, M, NT> twp(tw);
   const int p = blockIdx.y;
   const int64_t row0 = (int64_t)blockIdx.x * L;
   const int64_t nrows = (int64_t)N * N;
   const T2* src = S1 + (int64_t)p * nrows * M;
-  constexpr int NT = L * Shape<R1, R2>::RMAX;
   constexpr int ESP = (L * M + NT - 1) / NT;
   {
     T2 vin[ESP];
@@ -319,6 +351,7 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
       if (i < L * M && r < nrows) vin[e] = src[r * M + i % M];
       else vin[e].x = vin[e].y = 0;
     }
+    twp.store(tws);
 #pragma unroll
     for (int e = 0; e < ESP; ++e) {
       const int i = threadIdx.x + e * NT;
