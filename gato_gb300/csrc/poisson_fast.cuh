@@ -191,6 +191,104 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   }
 }
 
+// The inputs a launch group of pair fields reads, staged once per CTA by
+// k_rows_fwd_multi: slot_of[i] is input i's staging slot (-1: unused).
+struct RowsIn {
+  int nin = 0;
+  int8_t idx[kMaxIn] = {};
+  int8_t slot_of[kMaxIn] = {};
+};
+
+// z forward for every field of a launch group: the L rows of each distinct
+// input (the orbitals, psi) are staged in shared memory once, then each field's
+// pair densities are formed straight into the stage-1 registers of its FFT.
+// Same transform and output as k_rows_fwd, without re-reading the inputs per
+// field. Staged rows are padded to N + 1 so the 16 lines a warp reads in stage 1
+// fall in different banks.
+template <typename T, int R1, int R2, int L>
+__global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
+    k_rows_fwd_multi(PassArgs args, RowsIn ri, int f0, int nfg, typename Cplx<T>::type* S1,
+                     const typename Cplx<T>::type* tw) {
+  using T2 = typename Cplx<T>::type;
+  constexpr int M = R1 * R2, N = M / 2, LP = L + 1, NP = N + 1;
+  constexpr int NT = L * Shape<R1, R2>::RMAX;
+  constexpr int EOUT = (L * M + NT - 1) / NT;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T2* buf = reinterpret_cast<T2*>(smraw);
+  T2* tws = buf + M * LP;
+  T* stage = reinterpret_cast<T*>(tws + M);   // [slot][line][z], rows of NP
+  const TwPrefetch<T2, M, NT> twp(tw);
+  const int64_t row0 = (int64_t)blockIdx.x * L;
+  const int64_t nrows = (int64_t)N * N;
+  // staging: 8 loads in flight per thread per batch
+  const int nel = ri.nin * L * N;
+  constexpr int B = 8;
+  for (int base = 0; base < nel; base += B * NT) {
+    T v[B];
+#pragma unroll
+    for (int k = 0; k < B; ++k) {
+      const int i = base + threadIdx.x + k * NT;
+      const int sl = i / (L * N), rem = i % (L * N);
+      const int64_t r = row0 + rem / N;
+      v[k] = (i < nel && r < nrows) ? reinterpret_cast<const T*>(args.in[ri.idx[sl]])[r * N + rem % N] : (T)0;
+    }
+#pragma unroll
+    for (int k = 0; k < B; ++k) {
+      const int i = base + threadIdx.x + k * NT;
+      if (i < nel) {
+        const int sl = i / (L * N), rem = i % (L * N);
+        stage[(sl * L + rem / N) * NP + rem % N] = v[k];
+      }
+    }
+  }
+  twp.store(tws);
+  __syncthreads();
+  const int t = threadIdx.x, line = t % L, q = t / L;
+  for (int p = 0; p < nfg; ++p) {
+    const FieldDesc& fd = args.f[f0 + p];
+    const int a0 = ri.slot_of[fd.p[0].a];
+    const int b0 = fd.p[0].b >= 0 ? ri.slot_of[fd.p[0].b] : -1;
+    const int a1 = fd.p[1].a >= 0 ? ri.slot_of[fd.p[1].a] : -1;
+    const int b1 = (a1 >= 0 && fd.p[1].b >= 0) ? ri.slot_of[fd.p[1].b] : -1;
+    if (q < R2) {
+      T2 v[R1];
+#pragma unroll
+      for (int n1 = 0; n1 < R1 / 2; ++n1) {
+        const int z = R2 * n1 + q;
+        T x = stage[(a0 * L + line) * NP + z];
+        if (b0 >= 0) x *= stage[(b0 * L + line) * NP + z];
+        T y = (T)0;
+        if (a1 >= 0) {
+          y = stage[(a1 * L + line) * NP + z];
+          if (b1 >= 0) y *= stage[(b1 * L + line) * NP + z];
+        }
+        v[n1].x = x;
+        v[n1].y = y;
+      }
+      rdft_half<T2, R1, -1>(v);
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) buf[(q * R1 + k1) * LP + line] = v[k1];
+    }
+    __syncthreads();
+    T2 X[R2];
+    if (q < R1) fwd_stage2<T2, R1, R2>(buf, LP, line, q, tws, X);
+    __syncthreads();
+    if (q < R1)
+#pragma unroll
+      for (int k2 = 0; k2 < R2; ++k2) buf[(q + R1 * k2) * LP + line] = X[k2];
+    __syncthreads();
+    T2* dst = S1 + (int64_t)p * nrows * M;
+#pragma unroll
+    for (int e = 0; e < EOUT; ++e) {
+      const int i = threadIdx.x + e * NT;
+      const int ln = i / M, kz = i % M;
+      const int64_t r = row0 + ln;
+      if (i < L * M && r < nrows) dst[r * M + kz] = buf[kz * LP + ln];
+    }
+    __syncthreads();   // buf is rewritten by the next field
+  }
+}
+
 // z inverse over every field of the group, then the epilogue. NO > 0: the
 // accumulation terms target outputs < NO, kept in registers (each thread owns
 // EPT fixed (row, z) elements); NO == 0: energy mode.
@@ -221,6 +319,28 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   for (int p = 0; p < nfg; ++p) {
     const FieldDesc& fd = args.f[f0 + p];
     const T2* src = S1 + (int64_t)p * nrows * M;
+    // The epilogue's first field factor of each part (in[tc] of term 0, or the
+    // density in energy mode) does not depend on the transform: load it now so
+    // its latency overlaps the FFT instead of following it. A second term
+    // (block applies on the generic engine only) still loads in the epilogue.
+    T fac[EPT][2];
+#pragma unroll
+    for (int e = 0; e < EPT; ++e) {
+      const int i = e * NT + t;
+      const int64_t r = row0 + i / N;
+      const bool ok = i < L * N && r < nrows;
+      const int64_t gi = r * N + i % N;
+#pragma unroll
+      for (int qq = 0; qq < 2; ++qq) {
+        const PartDesc& d = fd.p[qq];
+        if constexpr (ENERGY)
+          fac[e][qq] = (ok && d.a >= 0) ? dens<T>(d, args.in, gi) : (T)0;
+        else
+          fac[e][qq] = (ok && d.a >= 0 && d.nt > 0)
+                           ? (d.tc[0] >= 0 ? reinterpret_cast<const T*>(args.in[d.tc[0]])[gi] : (T)1)
+                           : (T)0;
+      }
+    }
     // loads in batches of at most 8 elements per thread (the accumulators
     // already hold NO x EPT registers); the first batch is in flight across
     // the barrier that frees buf
@@ -281,13 +401,16 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
         if (d.a < 0) continue;
         const T val = qq == 0 ? J.x : J.y;
         if constexpr (ENERGY) {
-          const T de = dens<T>(d, args.in, gi);
+          const T de = fac[e][qq];
           if (d.eslot == 0) e0.add_prod(de * (T)d.ew, val);
           else e1.add_prod(de * (T)d.ew, val);
         } else {
-          for (int k = 0; k < d.nt; ++k) {
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            if (k >= d.nt) break;
             T m = (T)d.coef[k];
-            if (d.tc[k] >= 0) m *= reinterpret_cast<const T*>(args.in[d.tc[k]])[gi];
+            if (k == 0) m *= fac[e][qq];
+            else if (d.tc[1] >= 0) m *= reinterpret_cast<const T*>(args.in[d.tc[1]])[gi];
             const int to = d.to[k];
 #pragma unroll
             for (int o = 0; o < NO; ++o)
@@ -431,6 +554,32 @@ struct Launch {
     return GATO_OK;
   }
   static int rows_fwd(const PassArgs& a, int f0, int nfg, T2* S1, const T2* tw, cudaStream_t s) {
+    // three or more fields over few distinct inputs: stage the inputs once per
+    // CTA (with two fields, as in the matvec exchange, the per-field kernel's
+    // higher occupancy wins: 36 against 46 us at 128^3)
+    RowsIn ri;
+    for (int i = 0; i < kMaxIn; ++i) ri.slot_of[i] = -1;
+    auto use = [&](int idx) {
+      if (idx < 0 || ri.slot_of[idx] >= 0) return;
+      ri.slot_of[idx] = (int8_t)ri.nin;
+      ri.idx[ri.nin++] = (int8_t)idx;
+    };
+    for (int p = 0; p < nfg; ++p)
+      for (int qq = 0; qq < 2; ++qq) {
+        const PartDesc& d = a.f[f0 + p].p[qq];
+        if (d.a < 0) continue;
+        use(d.a);
+        use(d.b);
+      }
+    const size_t stage_bytes = (size_t)ri.nin * L * (N + 1) * sizeof(T);
+    if (nfg >= 3 && stage_bytes <= 48 * 1024) {
+      const size_t sm = sm_rows() + stage_bytes;
+      GATO_TRY(smem_attr(k_rows_fwd_multi<T, R1, R2, L>, sm));
+      const int64_t nrows = (int64_t)N * N;
+      k_rows_fwd_multi<T, R1, R2, L><<<(unsigned)((nrows + L - 1) / L), NT, sm, s>>>(a, ri, f0, nfg, S1, tw);
+      GATO_LAUNCH_TRY();
+      return GATO_OK;
+    }
     const size_t sm = sm_rows();
     GATO_TRY(smem_attr(k_rows_fwd<T, R1, R2, L>, sm));
     const int64_t nrows = (int64_t)N * N;
