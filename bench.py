@@ -34,7 +34,7 @@ sys.path.insert(0, ROOT)
 N_DEFAULT, H_DEFAULT, N_OCC = 128, 0.25, 4
 # DRAM read + write of one x-pass launch (5 fields, 128^3) in the ncu capture
 # summarised in profiles/block_fock_apply_h2o128_f32_kernels.md
-FMI_TRAFFIC_128 = 345_278_976 + 275_794_432
+FMI_TRAFFIC_128 = 345_434_624 + 276_196_864
 METRIC = "H2O 128^3 RHF block Fock-applies/s (mixed FP32/FP64 at |dE|<1uHa) and force time"
 UNIT = "Fock-applies/s"
 
