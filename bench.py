@@ -524,15 +524,27 @@ def run_profile(args):
     op.set_nonlocal(nonlocal_for(nuc, el, g, dtype))
     op.set_exchange(plan, fields)
     out = torch.empty_like(fields)
-    step = (lambda: op.apply_block(out)) if args.profile == "block" else (lambda: op.apply(fields[0], out[0]))
+    if args.profile == "scf":
+        # two mixed SCF iterations of the 128^3 water from the seeded orbitals (the C3 inner loop)
+        from gato_gb300.physics.water import solve_rhf_at_geometry
+        init = torch.tensor(orbs, device="cuda").permute(1, 2, 3, 0)
+        step = lambda: solve_rhf_at_geometry(nuc, el, g, precision="mixed", max_iters=2,   # noqa: E731
+                                             initial_orbitals=init)
+    elif args.profile == "block":
+        step = lambda: op.apply_block(out)   # noqa: E731
+    else:
+        step = lambda: op.apply(fields[0], out[0])   # noqa: E731
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
     n0 = _lib.launch_count()
+    t0 = time.perf_counter()
     for _ in range(args.steps):
         step()
     torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
     print(json.dumps({"profile": args.profile, "dtype": args.profile_dtype, "N": N, "steps": args.steps,
+                      "ms_per_step": 1e3 * dt / args.steps,
                       "launches_per_step": (_lib.launch_count() - n0) / args.steps}), flush=True)
 
 
@@ -551,8 +563,8 @@ def main():
     ap.add_argument("--impl", default="gato", choices=["gato", "reference"])
     ap.add_argument("--N", type=int, default=N_DEFAULT)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--profile", default=None, choices=["block", "matvec"],
-                    help="run only the block / matvec Fock apply (for ncu captures)")
+    ap.add_argument("--profile", default=None, choices=["block", "matvec", "scf"],
+                    help="run only the block / matvec Fock apply or two SCF iterations (for ncu captures)")
     ap.add_argument("--profile-dtype", default="f32", choices=["f32", "f64"])
     args = ap.parse_args()
     if args.warmup < 3:

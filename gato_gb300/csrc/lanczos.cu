@@ -64,6 +64,22 @@ __device__ __forceinline__ T pre_load(const T* W, const Pre<T>& p, const T* sc, 
 // c_k is a cancellation sum (nearly orthogonal vectors), so its error scales
 // with |w|, not with c_k, and FP32 products would leave 1e-9-level components
 // in an FP64 basis.
+// Each block owns one contiguous, equal share of the n elements (rounded to
+// whole warps), walked in chunks of kChunk; basis vectors go four at a time
+// so every thread has 4 * kEPT independent loads in flight per step.
+__device__ __forceinline__ void block_range(int64_t n, int64_t& lo, int64_t& hi) {
+  int64_t per = (n + gridDim.x - 1) / gridDim.x;
+  per = (per + 31) / 32 * 32;
+  lo = (int64_t)blockIdx.x * per;
+  hi = lo + per < n ? lo + per : n;
+}
+
+template <typename C>
+__device__ __forceinline__ double warp_total(C v) {
+  if constexpr (sizeof(C) == 4) return (double)warp_sumf(v);
+  else return warp_sum(v);
+}
+
 template <typename T, typename C>
 __global__ void __launch_bounds__(kLzThreads)
     k_gemv_t(const T* __restrict__ V, int64_t ld, int nk, const T* __restrict__ W, Pre<T> pre,
@@ -74,24 +90,42 @@ __global__ void __launch_bounds__(kLzThreads)
   pre_scalars(pre, sc);
   for (int i = threadIdx.x; i < nw * nk; i += blockDim.x) wacc[i] = 0.0;
   __syncthreads();
-  for (int64_t base = (int64_t)blockIdx.x * kChunk; base < n; base += (int64_t)gridDim.x * kChunk) {
+  int64_t lo, hi;
+  block_range(n, lo, hi);
+  for (int64_t base = lo; base < hi; base += kChunk) {
     C w[kEPT];
 #pragma unroll
     for (int e = 0; e < kEPT; ++e) {
       const int64_t i = base + e * kLzThreads + threadIdx.x;
-      w[e] = i < n ? (C)pre_load(W, pre, sc, i) : (C)0;
+      w[e] = i < hi ? (C)pre_load(W, pre, sc, i) : (C)0;
     }
-    for (int k = 0; k < nk; ++k) {
+    int k = 0;
+    for (; k + 4 <= nk; k += 4) {
+      C sk[4] = {(C)0, (C)0, (C)0, (C)0};
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const T* vk = V + (int64_t)(k + u) * ld;
+#pragma unroll
+        for (int e = 0; e < kEPT; ++e) {
+          const int64_t i = base + e * kLzThreads + threadIdx.x;
+          if (i < hi) sk[u] = fma((C)vk[i], w[e], sk[u]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const double d = warp_total<C>(sk[u]);
+        if (lane == 0) wacc[warp * nk + k + u] += d;
+      }
+    }
+    for (; k < nk; ++k) {
       const T* vk = V + (int64_t)k * ld;
-      C s = (C)0;
+      C sk = (C)0;
 #pragma unroll
       for (int e = 0; e < kEPT; ++e) {
         const int64_t i = base + e * kLzThreads + threadIdx.x;
-        if (i < n) s = fma((C)vk[i], w[e], s);
+        if (i < hi) sk = fma((C)vk[i], w[e], sk);
       }
-      double d;
-      if constexpr (sizeof(C) == 4) d = (double)warp_sumf(s);
-      else d = warp_sum(s);
+      const double d = warp_total<C>(sk);
       if (lane == 0) wacc[warp * nk + k] += d;
     }
   }
@@ -120,28 +154,49 @@ __global__ void __launch_bounds__(kLzThreads)
   T sc[2];
   pre_scalars(pre, sc);
   Acc<T> acc;
-  for (int64_t base = (int64_t)blockIdx.x * kChunk; base < n; base += (int64_t)gridDim.x * kChunk) {
+  int64_t lo, hi;
+  block_range(n, lo, hi);
+  for (int64_t base = lo; base < hi; base += kChunk) {
     T w[kEPT];
     C corr[kEPT];
 #pragma unroll
     for (int e = 0; e < kEPT; ++e) {
       const int64_t i = base + e * kLzThreads + threadIdx.x;
-      w[e] = i < n ? pre_load(W, pre, sc, i) : (T)0;
+      w[e] = i < hi ? pre_load(W, pre, sc, i) : (T)0;
       corr[e] = (C)0;
     }
-    for (int k = 0; k < nk; ++k) {
+    int k = 0;
+    for (; k + 4 <= nk; k += 4) {
+      C v[4][kEPT];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const T* vk = V + (int64_t)(k + u) * ld;
+#pragma unroll
+        for (int e = 0; e < kEPT; ++e) {
+          const int64_t i = base + e * kLzThreads + threadIdx.x;
+          v[u][e] = i < hi ? (C)vk[i] : (C)0;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const C ck = (C)cs[k + u];
+#pragma unroll
+        for (int e = 0; e < kEPT; ++e) corr[e] = fma(ck, v[u][e], corr[e]);
+      }
+    }
+    for (; k < nk; ++k) {
       const T* vk = V + (int64_t)k * ld;
       const C ck = (C)cs[k];
 #pragma unroll
       for (int e = 0; e < kEPT; ++e) {
         const int64_t i = base + e * kLzThreads + threadIdx.x;
-        if (i < n) corr[e] = fma(ck, (C)vk[i], corr[e]);
+        if (i < hi) corr[e] = fma(ck, (C)vk[i], corr[e]);
       }
     }
 #pragma unroll
     for (int e = 0; e < kEPT; ++e) {
       const int64_t i = base + e * kLzThreads + threadIdx.x;
-      if (i < n) {
+      if (i < hi) {
         w[e] -= (T)corr[e];
         W[i] = w[e];
         acc.add_prod(w[e], w[e]);
@@ -364,7 +419,8 @@ struct LzScratch {
   int nblk;
 };
 
-inline int lz_nblk(int64_t n) { return (int)std::min<int64_t>((n + kChunk - 1) / kChunk, 2 * 152 * 2); }
+// one resident wave: k_gemv_n holds 3 blocks of kLzThreads per SM (80 registers)
+inline int lz_nblk(int64_t n) { return (int)std::min<int64_t>((n + kChunk - 1) / kChunk, 3 * 152); }
 
 int lz_scratch(cudaStream_t s, int64_t n, int m, int K, LzScratch& z) {
   z.nblk = lz_nblk(n);
