@@ -169,7 +169,10 @@ __global__ void k_wdot_partials(const T* __restrict__ a, const T* __restrict__ w
 
 template <typename T>
 __global__ void k_normalize(T* a, int64_t n, const double* nsq) {
-  double s = 1.0 / sqrt(nsq[0]);
+  __shared__ double sc;   // one FP64 reciprocal square root per block
+  if (threadIdx.x == 0) sc = 1.0 / sqrt(nsq[0]);
+  __syncthreads();
+  const double s = sc;
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
     a[i] = (T)((double)a[i] * s);

@@ -27,7 +27,10 @@ __global__ void k_one_minus_dt_v(const T* __restrict__ V, T* Vp, int64_t n, doub
 // dst = src / sqrt(nsq[0]); src may alias dst
 template <typename T>
 __global__ void k_scale_rsqrt(const T* src, T* dst, int64_t n, const double* nsq) {
-  const double s = 1.0 / sqrt(nsq[0]);
+  __shared__ double sc;   // one FP64 reciprocal square root per block
+  if (threadIdx.x == 0) sc = 1.0 / sqrt(nsq[0]);
+  __syncthreads();
+  const double s = sc;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     dst[i] = (T)((double)src[i] * s);

@@ -208,11 +208,19 @@ __global__ void __launch_bounds__(kLzThreads)
 }
 
 // beta = sqrt(nrm); v = W / beta (or 0); betas_out[0] = beta
+// (the square root and the reciprocal are FP64 and cost many FP64-pipe
+// instructions on GB300, so one thread per block computes them)
 template <typename T>
 __global__ void k_beta_scale(T* W, int64_t n, const double* nrm, double* beta_out) {
-  const double beta = sqrt(nrm[0]);
-  if (blockIdx.x == 0 && threadIdx.x == 0) beta_out[0] = beta;
-  const double inv = beta > 0 ? 1.0 / beta : 0.0;
+  __shared__ double sb[2];
+  if (threadIdx.x == 0) {
+    const double beta = sqrt(nrm[0]);
+    sb[0] = beta;
+    sb[1] = beta > 0 ? 1.0 / beta : 0.0;
+    if (blockIdx.x == 0) beta_out[0] = beta;
+  }
+  __syncthreads();
+  const double beta = sb[0], inv = sb[1];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     W[i] = beta > 0 ? (T)((double)W[i] * inv) : (T)0;
@@ -220,7 +228,10 @@ __global__ void k_beta_scale(T* W, int64_t n, const double* nrm, double* beta_ou
 
 template <typename T>
 __global__ void k_scale_copy(const T* __restrict__ src, T* dst, int64_t n, const double* nrm) {
-  const double inv = 1.0 / sqrt(nrm[0]);
+  __shared__ double sc;   // one FP64 reciprocal square root per block
+  if (threadIdx.x == 0) sc = 1.0 / sqrt(nrm[0]);
+  __syncthreads();
+  const double inv = sc;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     dst[i] = (T)((double)src[i] * inv);
@@ -416,20 +427,28 @@ __global__ void __launch_bounds__(256) k_ritz(const T* __restrict__ V, int64_t l
 
 struct LzScratch {
   double *part, *coef, *nrm, *Y, *work;
-  int nblk;
+  int nblk;     // k_gemv_n grid
+  int nblk_t;   // k_gemv_t grid
 };
 
-// one resident wave: k_gemv_n holds 3 blocks of kLzThreads per SM (80 registers)
+// One resident wave each: k_gemv_n holds 3 blocks of kLzThreads per SM (80
+// registers); k_gemv_t, which is bound by memory latency, runs as many as its
+// registers allow (48 FP32 / 62 FP64: 5 / 4 blocks) to keep more loads in flight.
 inline int lz_nblk(int64_t n) { return (int)std::min<int64_t>((n + kChunk - 1) / kChunk, 3 * 152); }
+inline int lz_nblk_t(int64_t n, bool fp64) {
+  return (int)std::min<int64_t>((n + kChunk - 1) / kChunk, (fp64 ? 4 : 5) * 152);
+}
 
-int lz_scratch(cudaStream_t s, int64_t n, int m, int K, LzScratch& z) {
+int lz_scratch(cudaStream_t s, int64_t n, int m, int K, LzScratch& z, bool fp64) {
   z.nblk = lz_nblk(n);
-  // partials (m+1)*nblk, coefficients (m+1), norm, Y (m*K), LU work 5*m*K
-  const size_t need = ((size_t)(m + 1) * z.nblk + (m + 1) + 8 + (size_t)m * K + (size_t)5 * m * K) *
+  z.nblk_t = lz_nblk_t(n, fp64);
+  const int np = std::max(z.nblk, z.nblk_t);
+  // partials (m+1)*max(grids), coefficients (m+1), norm, Y (m*K), LU work 5*m*K
+  const size_t need = ((size_t)(m + 1) * np + (m + 1) + 8 + (size_t)m * K + (size_t)5 * m * K) *
                       sizeof(double);
   z.part = (double*)stream_scratch(s, need, kSlotLanczos);
   if (!z.part) return fail(GATO_ENOMEM, "lanczos: scratch allocation failed");
-  z.coef = z.part + (size_t)(m + 1) * z.nblk;
+  z.coef = z.part + (size_t)(m + 1) * np;
   z.nrm = z.coef + (m + 1);
   z.Y = z.nrm + 8;
   z.work = z.Y + (size_t)m * K;
@@ -467,17 +486,18 @@ int lz_step(T* Vb, int64_t n, double dV, int j, int passes, double* alphas, doub
   if (smt > 48 * 1024)
     GATO_CUDA_TRY(cudaFuncSetAttribute(k_gemv_t<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt));
   // alpha_j = dV <v_j, w'>
-  k_gemv_t<T, T><<<z.nblk, kLzThreads, (kLzThreads / 32) * sizeof(double), s>>>(vj, n, 1, W, p1, n, z.part);
+  k_gemv_t<T, T><<<z.nblk_t, kLzThreads, (kLzThreads / 32) * sizeof(double), s>>>(vj, n, 1, W, p1, n,
+                                                                                  z.part);
   GATO_LAUNCH_TRY();
-  GATO_TRY(finalize_sums(z.part, 1, z.nblk, dV, alphas + j, s));
+  GATO_TRY(finalize_sums(z.part, 1, z.nblk_t, dV, alphas + j, s));
   Pre<T> p2 = p1;
   p2.u[1] = vj;
   p2.s[1] = alphas + j;
   for (int p = 0; p < passes; ++p) {
     const Pre<T>& pp = p == 0 ? p2 : Pre<T>();
-    k_gemv_t<T, T><<<z.nblk, kLzThreads, smt, s>>>(Vb, n, nk, W, pp, n, z.part);
+    k_gemv_t<T, T><<<z.nblk_t, kLzThreads, smt, s>>>(Vb, n, nk, W, pp, n, z.part);
     GATO_LAUNCH_TRY();
-    GATO_TRY(finalize_sums(z.part, nk, z.nblk, dV, z.coef, s));
+    GATO_TRY(finalize_sums(z.part, nk, z.nblk_t, dV, z.coef, s));
     k_gemv_n<T, float><<<z.nblk, kLzThreads, smn, s>>>(Vb, n, nk, W, pp, z.coef, n, z.part);
     GATO_LAUNCH_TRY();
   }
@@ -515,7 +535,7 @@ int lanczos_typed(gato_operator& op, const void* psi0, int m, int K, double tol,
   const int64_t n = op_n3(op);
   T* Vb = (T*)krylov;
   LzScratch z;
-  GATO_TRY(lz_scratch(s, n, m, K, z));
+  GATO_TRY(lz_scratch(s, n, m, K, z, sizeof(T) == 8));
   GATO_TRY(lz_begin<T>(psi0, Vb, n, op.dV, z, s));
   for (int j = 0; j < m; ++j) {
     GATO_TRY(op_apply(op, Vb + (int64_t)j * n, Vb + (int64_t)(j + 1) * n, s));
@@ -551,7 +571,7 @@ extern "C" int gato_lanczos_begin(int dtype, int64_t n, double dV, const void* p
   if (!psi0 || !krylov || n < 1 || m < 1 || K < 1 || K > m) return fail(GATO_EBADARG, "gato_lanczos_begin: bad arguments");
   cudaStream_t s = as_stream(stream);
   LzScratch z;
-  GATO_TRY(lz_scratch(s, n, m, K, z));
+  GATO_TRY(lz_scratch(s, n, m, K, z, dtype == GATO_F64));
   if (dtype == GATO_F64) return lz_begin<double>(psi0, (double*)krylov, n, dV, z, s);
   return lz_begin<float>(psi0, (float*)krylov, n, dV, z, s);
 }
@@ -563,7 +583,7 @@ extern "C" int gato_lanczos_step(int dtype, int64_t n, double dV, void* krylov, 
   if (reorth_passes < 1 || reorth_passes > 2) return fail(GATO_EBADARG, "reorth_passes must be 1 or 2");
   cudaStream_t s = as_stream(stream);
   LzScratch z;
-  GATO_TRY(lz_scratch(s, n, m, K, z));
+  GATO_TRY(lz_scratch(s, n, m, K, z, dtype == GATO_F64));
   if (dtype == GATO_F64) return lz_step<double>((double*)krylov, n, dV, j, reorth_passes, alphas_dev, betas_dev, z, s);
   return lz_step<float>((float*)krylov, n, dV, j, reorth_passes, alphas_dev, betas_dev, z, s);
 }
@@ -575,7 +595,7 @@ extern "C" int gato_lanczos_finish(int dtype, int64_t n, const void* krylov, int
     return fail(GATO_EBADARG, "gato_lanczos_finish: bad arguments");
   cudaStream_t s = as_stream(stream);
   LzScratch z;
-  GATO_TRY(lz_scratch(s, n, m, K, z));
+  GATO_TRY(lz_scratch(s, n, m, K, z, dtype == GATO_F64));
   if (dtype == GATO_F64)
     return lz_finish<double>((const double*)krylov, n, m, K, tol, alphas_dev, betas_dev, evals_dev, (double*)evecs, flag_dev, z, s);
   return lz_finish<float>((const float*)krylov, n, m, K, tol, alphas_dev, betas_dev, evals_dev, (float*)evecs, flag_dev, z, s);
