@@ -20,9 +20,12 @@
 // eigenvectors by inverse iteration with the partial-pivoting tridiagonal LU
 // (the LAPACK dgttrf/dgtts2 scheme), re-orthogonalised within clusters of
 // close eigenvalues. Ritz vectors are sum_j Y[j,k] v_j.
+#include <atomic>
 #include <cmath>
+#include <type_traits>
 
 #include "op.cuh"
+#include "ptx.cuh"
 
 namespace gato {
 int dot_impl(int dtype, const void* a, const void* b, int64_t n, double scale, double* out,
@@ -205,6 +208,244 @@ __global__ void __launch_bounds__(kLzThreads)
   }
   const double s = block_sum(acc.value(), sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// ---- bulk-copy streaming versions of the two sweeps ----------------------------
+// The basis vectors are the bulk of the Lanczos traffic. Here each block owns
+// an equal element range; a producer warp's lane 0 streams the items (chunk c,
+// vector k) of that range, chunk-major, as contiguous 1-D bulk copies into a
+// kBulkStages ring (one "full" mbarrier per stage with the byte count, one
+// "empty" mbarrier with one arrival per consumer warp). The eight consumer
+// warps read each item from shared memory as 16-byte vectors, release the stage
+// at once, and do the arithmetic in registers: the memory parallelism lives
+// in the ring (48 KB per block) instead of in registers. Used when every
+// vector starts on a 16-byte boundary and n * sizeof(T) is a multiple of 16.
+constexpr int kBulkStages = 6;   // 48 KB of ring per block: 3 blocks per SM
+constexpr int kBulkWarps = 8;                           // consumer warps
+constexpr int kBulkThreads = 32 * (kBulkWarps + 1);     // + the producer warp
+
+template <typename T>
+struct BulkGeom {
+  static constexpr int VEC = 16 / (int)sizeof(T);          // elements per 16-byte vector
+  static constexpr int CH = sizeof(T) == 4 ? 2048 : 1024;  // elements per item (8 KB)
+  static constexpr int GRP = CH / (32 * kBulkWarps * VEC); // vectors per thread per item (2)
+  static constexpr int EPT = GRP * VEC;
+  // element u of group g of consumer thread ct sits at g * (256 VEC) + ct VEC + u
+  __device__ static int idx(int ct, int g, int u) { return g * (32 * kBulkWarps * VEC) + ct * VEC + u; }
+};
+
+template <typename T>
+__device__ __forceinline__ void bulk_producer(const T* V, int64_t ld, int nk, int64_t lo, int64_t hi,
+                                              int items, T* stage, uint64_t* full, uint64_t* empty,
+                                              volatile int* abort_v, int* err) {
+  using G = BulkGeom<T>;
+  int t = 0, c = 0, k = 0;
+  for (; t < items; ++t) {
+    const int sl = t % kBulkStages;
+    if (t >= kBulkStages &&
+        !mbar_wait_bounded(&empty[sl], (uint32_t)(((t / kBulkStages) - 1) & 1), err, 105)) {
+      *abort_v = 1;
+      break;
+    }
+    if (*abort_v) break;
+    const int64_t base = lo + (int64_t)c * G::CH;
+    const int64_t cnt = hi - base < G::CH ? hi - base : G::CH;
+    const uint32_t bytes = (uint32_t)(cnt * sizeof(T));
+    mbar_expect_tx(&full[sl], bytes);
+    bulk_load(stage + (size_t)sl * G::CH, V + (int64_t)k * ld + base, bytes, &full[sl]);
+    if (++k == nk) {
+      k = 0;
+      ++c;
+    }
+  }
+  if (*abort_v)   // let the copies in flight land (bounded) before the block exits
+    for (int p = t > kBulkStages ? t - kBulkStages : 0; p < t; ++p)
+      mbar_wait_bounded(&full[p % kBulkStages], (uint32_t)((p / kBulkStages) & 1), err, 106);
+}
+
+// Warp-uniform wait for item t; false (and the abort flag set) if it timed out.
+__device__ __forceinline__ bool bulk_wait(uint64_t* full, int t, volatile int* abort_v, int* err) {
+  bool fail = *abort_v != 0;
+  if (!fail) fail = !mbar_wait_bounded(&full[t % kBulkStages], (uint32_t)((t / kBulkStages) & 1), err, 107);
+  if (__any_sync(0xffffffffu, fail)) {
+    if ((threadIdx.x & 31) == 0) *abort_v = 1;
+    return false;
+  }
+  return true;
+}
+
+// k_gemv_t with bulk streaming: part[k * gridDim.x + block] = sum_i V_k[i] w[i]
+template <typename T>
+__global__ void __launch_bounds__(kBulkThreads)
+    k_gemv_t_bulk(const T* __restrict__ V, int64_t ld, int nk, const T* __restrict__ W, Pre<T> pre,
+                  int64_t n, double* part, int* err) {
+  using G = BulkGeom<T>;
+  using V4 = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  extern __shared__ __align__(128) unsigned char smb[];
+  T* stage = reinterpret_cast<T*>(smb);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smb + (size_t)kBulkStages * G::CH * sizeof(T));
+  uint64_t* empty = full + kBulkStages;
+  double* wacc = reinterpret_cast<double*>(empty + kBulkStages);   // [warp][k]
+  __shared__ int abort_flag;
+  volatile int* abort_v = &abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int64_t lo, hi;
+  block_range(n, lo, hi);
+  const int nch = hi > lo ? (int)((hi - lo + G::CH - 1) / G::CH) : 0;
+  const int items = nch * nk;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kBulkStages; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], kBulkWarps);
+    }
+    abort_flag = 0;
+    fence_barrier_init();
+  }
+  for (int i = threadIdx.x; i < kBulkWarps * nk; i += blockDim.x) wacc[i] = 0.0;
+  __syncthreads();
+  if (warp == kBulkWarps) {
+    if (lane == 0) bulk_producer<T>(V, ld, nk, lo, hi, items, stage, full, empty, abort_v, err);
+  } else {
+    const int ct = threadIdx.x;
+    T sc[2];
+    pre_scalars(pre, sc);
+    T w[G::EPT];
+    int c = 0, k = 0;
+    for (int t = 0; t < items; ++t) {
+      const int64_t base = lo + (int64_t)c * G::CH;
+      if (k == 0) {
+#pragma unroll
+        for (int g = 0; g < G::GRP; ++g)
+#pragma unroll
+          for (int u = 0; u < G::VEC; ++u) {
+            const int64_t i = base + G::idx(ct, g, u);
+            w[g * G::VEC + u] = i < hi ? pre_load(W, pre, sc, i) : (T)0;
+          }
+      }
+      if (!bulk_wait(full, t, abort_v, err)) break;
+      const T* st = stage + (size_t)(t % kBulkStages) * G::CH;
+      T v[G::EPT];
+#pragma unroll
+      for (int g = 0; g < G::GRP; ++g) {
+        const V4 q = *reinterpret_cast<const V4*>(st + G::idx(ct, g, 0));
+        const T* qe = reinterpret_cast<const T*>(&q);
+#pragma unroll
+        for (int u = 0; u < G::VEC; ++u) v[g * G::VEC + u] = qe[u];
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[t % kBulkStages]);
+      T sk = (T)0;
+#pragma unroll
+      for (int g = 0; g < G::GRP; ++g)
+#pragma unroll
+        for (int u = 0; u < G::VEC; ++u)
+          if (base + G::idx(ct, g, u) < hi) sk = fma(v[g * G::VEC + u], w[g * G::VEC + u], sk);
+      const double d = warp_total<T>(sk);
+      if (lane == 0) wacc[warp * nk + k] += d;
+      if (++k == nk) {
+        k = 0;
+        ++c;
+      }
+    }
+  }
+  __syncthreads();
+  if (*abort_v) return;
+  for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+    double sum = 0.0;
+    for (int wp = 0; wp < kBulkWarps; ++wp) sum += wacc[wp * nk + k];
+    part[(int64_t)k * gridDim.x + blockIdx.x] = sum;
+  }
+}
+
+// k_gemv_n with bulk streaming: W <- W - pre - sum_k c_k v_k, norm partial
+// part[block]; the correction accumulates in FP32 as in k_gemv_n<T, float>.
+template <typename T>
+__global__ void __launch_bounds__(kBulkThreads)
+    k_gemv_n_bulk(const T* __restrict__ V, int64_t ld, int nk, T* __restrict__ W, Pre<T> pre,
+                  const double* __restrict__ c_in, int64_t n, double* part, int* err) {
+  using G = BulkGeom<T>;
+  using V4 = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  extern __shared__ __align__(128) unsigned char smb[];
+  T* stage = reinterpret_cast<T*>(smb);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smb + (size_t)kBulkStages * G::CH * sizeof(T));
+  uint64_t* empty = full + kBulkStages;
+  double* cs = reinterpret_cast<double*>(empty + kBulkStages);
+  __shared__ double sh[32];
+  __shared__ int abort_flag;
+  volatile int* abort_v = &abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int64_t lo, hi;
+  block_range(n, lo, hi);
+  const int nch = hi > lo ? (int)((hi - lo + G::CH - 1) / G::CH) : 0;
+  const int items = nch * nk;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kBulkStages; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], kBulkWarps);
+    }
+    abort_flag = 0;
+    fence_barrier_init();
+  }
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) cs[i] = c_in[i];
+  __syncthreads();
+  Acc<T> acc;
+  if (warp == kBulkWarps) {
+    if (lane == 0) bulk_producer<T>(V, ld, nk, lo, hi, items, stage, full, empty, abort_v, err);
+  } else {
+    const int ct = threadIdx.x;
+    T sc[2];
+    pre_scalars(pre, sc);
+    T w[G::EPT];
+    float corr[G::EPT];
+    int c = 0, k = 0;
+    for (int t = 0; t < items; ++t) {
+      const int64_t base = lo + (int64_t)c * G::CH;
+      if (k == 0) {
+#pragma unroll
+        for (int g = 0; g < G::GRP; ++g)
+#pragma unroll
+          for (int u = 0; u < G::VEC; ++u) {
+            const int64_t i = base + G::idx(ct, g, u);
+            w[g * G::VEC + u] = i < hi ? pre_load(W, pre, sc, i) : (T)0;
+            corr[g * G::VEC + u] = 0.f;
+          }
+      }
+      if (!bulk_wait(full, t, abort_v, err)) break;
+      const T* st = stage + (size_t)(t % kBulkStages) * G::CH;
+      T v[G::EPT];
+#pragma unroll
+      for (int g = 0; g < G::GRP; ++g) {
+        const V4 q = *reinterpret_cast<const V4*>(st + G::idx(ct, g, 0));
+        const T* qe = reinterpret_cast<const T*>(&q);
+#pragma unroll
+        for (int u = 0; u < G::VEC; ++u) v[g * G::VEC + u] = qe[u];
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[t % kBulkStages]);
+      const float ck = (float)cs[k];
+#pragma unroll
+      for (int e = 0; e < G::EPT; ++e) corr[e] = fmaf(ck, (float)v[e], corr[e]);
+      if (k == nk - 1) {
+#pragma unroll
+        for (int g = 0; g < G::GRP; ++g)
+#pragma unroll
+          for (int u = 0; u < G::VEC; ++u) {
+            const int64_t i = base + G::idx(ct, g, u);
+            if (i < hi) {
+              const T x = w[g * G::VEC + u] - (T)corr[g * G::VEC + u];
+              W[i] = x;
+              acc.add_prod(x, x);
+            }
+          }
+      }
+      if (++k == nk) {
+        k = 0;
+        ++c;
+      }
+    }
+  }
+  const double sum = block_sum(acc.value(), sh);
+  if (threadIdx.x == 0 && !*abort_v) part[blockIdx.x] = sum;
 }
 
 // beta = sqrt(nrm); v = W / beta (or 0); betas_out[0] = beta
@@ -429,6 +670,7 @@ struct LzScratch {
   double *part, *coef, *nrm, *Y, *work;
   int nblk;     // k_gemv_n grid
   int nblk_t;   // k_gemv_t grid
+  int nblk_b;   // bulk-streaming grid (both sweeps)
 };
 
 // One resident wave each: k_gemv_n holds 3 blocks of kLzThreads per SM (80
@@ -438,11 +680,17 @@ inline int lz_nblk(int64_t n) { return (int)std::min<int64_t>((n + kChunk - 1) /
 inline int lz_nblk_t(int64_t n, bool fp64) {
   return (int)std::min<int64_t>((n + kChunk - 1) / kChunk, (fp64 ? 4 : 5) * 152);
 }
+// bulk-streaming kernels: 3 blocks per SM (their ring is 48 KB), at least one item each
+inline int lz_nblk_b(int64_t n, bool fp64) {
+  const int64_t ch = fp64 ? BulkGeom<double>::CH : BulkGeom<float>::CH;
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + ch - 1) / ch, 3 * 152));
+}
 
 int lz_scratch(cudaStream_t s, int64_t n, int m, int K, LzScratch& z, bool fp64) {
   z.nblk = lz_nblk(n);
   z.nblk_t = lz_nblk_t(n, fp64);
-  const int np = std::max(z.nblk, z.nblk_t);
+  z.nblk_b = lz_nblk_b(n, fp64);
+  const int np = std::max(std::max(z.nblk, z.nblk_t), z.nblk_b);
   // partials (m+1)*max(grids), coefficients (m+1), norm, Y (m*K), LU work 5*m*K
   const size_t need = ((size_t)(m + 1) * np + (m + 1) + 8 + (size_t)m * K + (size_t)5 * m * K) *
                       sizeof(double);
@@ -470,6 +718,50 @@ int lz_begin(const void* psi0, T* Vb, int64_t n, double dV, const LzScratch& z, 
 // of w'' against v_0..v_j (reorth_passes times). Removing the large alpha_j
 // component before the projection keeps one classical pass as orthogonal as
 // the reference's modified Gram-Schmidt.
+// The bulk kernels need every basis vector on a 16-byte boundary.
+template <typename T>
+bool bulk_ok(const T* Vb, int64_t n) {
+  return ((uint64_t)n * sizeof(T)) % 16 == 0 && ((uintptr_t)Vb % 16) == 0;
+}
+
+template <typename K>
+int bulk_smem_attr(K kern, size_t bytes) {
+  // opt in to the carve-out once per device and size (the kernels take up to ~64 KB)
+  static std::atomic<unsigned> done{0};
+  int dev = 0;
+  GATO_CUDA_TRY(cudaGetDevice(&dev));
+  const unsigned bit = 1u << (dev & 31);
+  if (!(done.load() & bit)) {
+    GATO_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+    done.fetch_or(bit);
+  }
+  (void)bytes;
+  return GATO_OK;
+}
+
+template <typename T>
+int gemv_t_bulk(const T* V, int64_t ld, int nk, const T* W, const Pre<T>& pre, int64_t n, int nblk, double* part,
+                cudaStream_t s) {
+  const size_t sm = (size_t)kBulkStages * BulkGeom<T>::CH * sizeof(T) + 2 * kBulkStages * sizeof(uint64_t) +
+                    (size_t)kBulkWarps * nk * sizeof(double);
+  if (sm > 100 * 1024) return fail(GATO_EUNSUPPORTED, "lanczos: Krylov dimension too large for the bulk sweep");
+  GATO_TRY(bulk_smem_attr(k_gemv_t_bulk<T>, sm));
+  k_gemv_t_bulk<T><<<nblk, kBulkThreads, sm, s>>>(V, ld, nk, W, pre, n, part, device_error_word());
+  GATO_LAUNCH_TRY();
+  return GATO_OK;
+}
+
+template <typename T>
+int gemv_n_bulk(const T* V, int64_t ld, int nk, T* W, const Pre<T>& pre, const double* c, int64_t n, int nblk,
+                double* part, cudaStream_t s) {
+  const size_t sm = (size_t)kBulkStages * BulkGeom<T>::CH * sizeof(T) + 2 * kBulkStages * sizeof(uint64_t) +
+                    (size_t)nk * sizeof(double);
+  GATO_TRY(bulk_smem_attr(k_gemv_n_bulk<T>, sm));
+  k_gemv_n_bulk<T><<<nblk, kBulkThreads, sm, s>>>(V, ld, nk, W, pre, c, n, part, device_error_word());
+  GATO_LAUNCH_TRY();
+  return GATO_OK;
+}
+
 template <typename T>
 int lz_step(T* Vb, int64_t n, double dV, int j, int passes, double* alphas, double* betas,
             const LzScratch& z, cudaStream_t s) {
@@ -481,6 +773,24 @@ int lz_step(T* Vb, int64_t n, double dV, int j, int passes, double* alphas, doub
     p1.s[0] = betas + (j - 1);
   }
   const int nk = j + 1;
+  if (bulk_ok(Vb, n)) {
+    // alpha_j = dV <v_j, w'>
+    GATO_TRY(gemv_t_bulk<T>(vj, n, 1, W, p1, n, z.nblk_b, z.part, s));
+    GATO_TRY(finalize_sums(z.part, 1, z.nblk_b, dV, alphas + j, s));
+    Pre<T> p2 = p1;
+    p2.u[1] = vj;
+    p2.s[1] = alphas + j;
+    for (int p = 0; p < passes; ++p) {
+      const Pre<T>& pp = p == 0 ? p2 : Pre<T>();
+      GATO_TRY(gemv_t_bulk<T>(Vb, n, nk, W, pp, n, z.nblk_b, z.part, s));
+      GATO_TRY(finalize_sums(z.part, nk, z.nblk_b, dV, z.coef, s));
+      GATO_TRY(gemv_n_bulk<T>(Vb, n, nk, W, pp, z.coef, n, z.nblk_b, z.part, s));
+    }
+    GATO_TRY(finalize_sums(z.part, 1, z.nblk_b, dV, z.nrm, s));
+    k_beta_scale<T><<<grid_for(n, 256), 256, 0, s>>>(W, n, z.nrm, betas + j);
+    GATO_LAUNCH_TRY();
+    return GATO_OK;
+  }
   const size_t smt = (size_t)(kLzThreads / 32) * nk * sizeof(double);
   const size_t smn = (size_t)nk * sizeof(double);
   if (smt > 48 * 1024)
