@@ -379,11 +379,11 @@ def run_workload(args):
         # concurrent streams vs one stream, FP64 continuation checks on the grids <= 96^3
         from gato_gb300.batch import draw_systems, fp64_check, solve_batch, summarize
         specs = draw_systems(48, seed=0)
-        res, wall = solve_batch(specs, precision="mixed", streams=args.streams, max_iters=80, tol=1e-8)
+        res, wall = solve_batch(specs, precision="mixed", streams=args.streams, max_iters=80, tol=1e-7)
         out["concurrent"] = summarize(res, wall)
         out["concurrent"]["streams"] = args.streams
         if args.c5_sequential:
-            res1, wall1 = solve_batch(specs, precision="mixed", streams=1, max_iters=80, tol=1e-8)
+            res1, wall1 = solve_batch(specs, precision="mixed", streams=1, max_iters=80, tol=1e-7)
             out["sequential_wall_s"] = wall1
             out["concurrency_speedup"] = wall1 / wall
             # same kernels on the same inputs: the two runs must agree bit for bit
@@ -437,7 +437,9 @@ def run_workload(args):
         if args.workload == "c3":
             nuc = water_initial_geometry(1.81, 104.5)
             nuc = type(nuc)(nuc.positions + torch.tensor(rng.uniform(-0.05, 0.05, (3, 3))), nuc.charges)
-            p32, t32 = _sync_time(lambda: solve_rhf_at_geometry(nuc, el, g, precision="mixed", tol=1e-8,
+            # the mixed SCF's energy noise floor is ~1e-8..1e-7 Ha (FP64 energies of orbitals from the
+            # FP32 Fock operator), so it stops at 1e-7; the FP64 continuation below goes to 1e-8
+            p32, t32 = _sync_time(lambda: solve_rhf_at_geometry(nuc, el, g, precision="mixed", tol=1e-7,
                                                                 max_iters=80))
             out["mixed"] = {"E": p32.energy, "iters": p32.n_iters, "converged": p32.converged, "scf_s": t32,
                             "orbital_energies": p32.orbital_energies.cpu().tolist()}

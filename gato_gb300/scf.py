@@ -295,12 +295,14 @@ def scf_rhf(V_ext, grid: Grid3D, n_occ: int, *, initial_orbitals=None, max_iters
     on the host. Everything between the two host reads runs on the device.
 
     With ``precision="mixed"`` the Fock operator, its exchange and the
-    eigensolve run on FP32 fields; the density, the mixing, V_H and the energy
-    run in FP64 on an FP64 copy of the new orbitals. An FP32 Hartree solve
-    carries a relative error near 1e-7 in E_H (about 2e-6 Ha for water), which
-    would be larger than the 1e-6 Ha agreement the two precisions are held
-    to; the FP64 part costs one FP64 density solve and one FP64 energy pass
-    per iteration against about m FP32 Fock applies.
+    eigensolve run on FP32 fields; the density, the mixing and V_H run in FP64
+    on an FP64 copy of the new orbitals. An FP32 Hartree solve carries a
+    relative error near 1e-7 in E_H (about 2e-6 Ha for water), larger than the
+    1e-6 Ha agreement the two precisions are held to, so the energy is FP64
+    wherever it decides anything: the FP32 energy terms serve only while
+    |E_k - E_{k-1}| > max(1e3 tol, 1e-4); from the first iterate below that,
+    every energy (and every convergence test) is FP64, and the returned energy
+    is always an FP64 evaluation.
     """
     dtype = precision_dtype(precision)
     mixed = dtype != torch.float64
@@ -345,6 +347,12 @@ def scf_rhf(V_ext, grid: Grid3D, n_occ: int, *, initial_orbitals=None, max_iters
     history: list[float] = []
     E_prev = float("inf")
     E = float("inf")
+    # Mixed precision: the FP32 energy terms carry ~1e-7 relative noise (up to ~1e-5 Ha on
+    # small grids), harmless while the energy still moves by more than `switch` per iteration;
+    # below that every energy (and so every convergence test) is FP64. The plain path is FP64
+    # throughout.
+    energy64 = not mixed
+    switch = max(1e3 * tol, 1e-4)
     orbital_energies = torch.zeros(n_occ, dtype=f64, device=dev)
     converged = False
     terms = None
@@ -370,13 +378,29 @@ def scf_rhf(V_ext, grid: Grid3D, n_occ: int, *, initial_orbitals=None, max_iters
         orb64 = convert(orb, buf64[: orb.shape[0]]) if mixed else orb
         _density_fields(orb64, rho_new)
         _lib.call("gato_mix", _lib.F64, P(rho), P(rho_new), n3, float(mixing), s())
-        terms = _energy_terms(orb64, V_ext64, grid, boundary, order, eps, V_nl_apply, op=op64)
-        E = float(terms.sum())
+        if energy64:
+            terms = _energy_terms(orb64, V_ext64, grid, boundary, order, eps, V_nl_apply, op=op64)
+            E = float(terms.sum())
+        else:
+            terms = _energy_terms(orb, V_ext, grid, boundary, order, eps, V_nl_apply, op=op)
+            E = float(terms.sum())
+            if abs(E - E_prev) < switch:
+                # close to the stop: from here on every energy is FP64, starting with this iterate
+                energy64 = True
+                terms = _energy_terms(orb64, V_ext64, grid, boundary, order, eps, V_nl_apply, op=op64)
+                E = float(terms.sum())
+                history.append(E)
+                E_prev = E
+                continue
         history.append(E)
-        if abs(E - E_prev) < tol:
+        if energy64 and abs(E - E_prev) < tol:
             converged = True
             break
         E_prev = E
+    if not energy64:
+        # max_iters reached on FP32 energies: the reported energy is still an FP64 evaluation
+        terms = _energy_terms(orb64, V_ext64, grid, boundary, order, eps, V_nl_apply, op=op64)
+        E = float(terms.sum())
     return SCFResult(from_fields(orb), E, orbital_energies, it, converged, history, terms)
 
 
