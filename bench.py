@@ -34,7 +34,7 @@ sys.path.insert(0, ROOT)
 N_DEFAULT, H_DEFAULT, N_OCC = 128, 0.25, 4
 # DRAM read + write of one x-pass launch (5 fields, 128^3) in the ncu capture
 # summarised in profiles/block_fock_apply_h2o128_f32_kernels.md
-FMI_TRAFFIC_128 = 345_434_624 + 276_196_864
+FMI_TRAFFIC_128 = 345_241_088 + 275_777_792
 METRIC = "H2O 128^3 RHF block Fock-applies/s (mixed FP32/FP64 at |dE|<1uHa) and force time"
 UNIT = "Fock-applies/s"
 
@@ -177,6 +177,57 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def cufft_comparator(st, N, h, eps, timed, steps):
+    """The reference's Hockney solve (solvers/poisson.py:47-57) on cuFFT through torch.fft, timed beside
+    this library's pipeline on the same FP32 inputs. Comparator only: J = irfftn(rfftn(pad(rho)) *
+    rfftn(G))[:N, :N, :N] dV with rfftn(G) built once (the reference rebuilds it on every call).
+    Reported: one Hartree solve both ways, and the 10 pair potentials J[phi_a phi_b] of a block apply
+    on cuFFT against this library's whole block apply (which also runs the stencil, the non-local part
+    and the exchange accumulation)."""
+    import torch
+    from gato_gb300.solvers.poisson import hartree_potential
+    from gato_gb300.grid import Grid3D
+    dev = st["fields"].device
+    M = 2 * N
+    idx = torch.arange(M, device=dev, dtype=torch.float64)
+    disp = torch.where(idx < N, idx * h, (idx - M) * h)
+    G = 1.0 / torch.sqrt(disp[:, None, None] ** 2 + disp[None, :, None] ** 2 + disp[None, None, :] ** 2 + eps * eps)
+    ghat = torch.fft.rfftn(G.to(torch.float32)) * (h ** 3)
+    del G
+    phi = st["fields"]
+    n = phi.shape[0]
+    pairs = [(a, b) for a in range(n) for b in range(a, n)]
+    pad = torch.zeros((len(pairs), M, M, M), dtype=torch.float32, device=dev)
+
+    def pair_solves():
+        for i, (a, b) in enumerate(pairs):
+            pad[i, :N, :N, :N] = phi[a] * phi[b]
+        J = torch.fft.irfftn(torch.fft.rfftn(pad, dim=(1, 2, 3)) * ghat, s=(M, M, M), dim=(1, 2, 3))
+        return J[:, :N, :N, :N].contiguous()
+
+    rho = (2.0 * (phi * phi).sum(0)).contiguous()
+    pad1 = torch.zeros((M, M, M), dtype=torch.float32, device=dev)
+
+    def hartree_cufft():
+        pad1[:N, :N, :N] = rho
+        return torch.fft.irfftn(torch.fft.rfftn(pad1) * ghat, s=(M, M, M))[:N, :N, :N].contiguous()
+
+    g = Grid3D(N, N * h)
+    t_pairs = timed(pair_solves, steps, 2)
+    t_hc = timed(hartree_cufft, steps, 2)
+    t_hg = timed(lambda: hartree_potential(rho, g, eps), steps, 2)
+    err = float(torch.max(torch.abs(hartree_cufft() - hartree_potential(rho, g, eps))) /
+                torch.max(torch.abs(hartree_cufft())))
+    out = {"hartree_us": {"gato": 1e6 * sum(t_hg) / len(t_hg), "cufft": 1e6 * sum(t_hc) / len(t_hc),
+                          "max_rel_diff": err},
+           "pair_potentials_10_us_cufft": 1e6 * sum(t_pairs) / len(t_pairs),
+           "note": "torch.fft (cuFFT) FP32 rfftn/irfftn of the zero-padded 2N^3 grid with a precomputed "
+                   "kernel spectrum; comparator only, never on the product path"}
+    del pad, pad1, ghat
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gato(args):
     import numpy as np
     import torch
@@ -299,9 +350,15 @@ def run_gato(args):
     from gato_gb300.operators import stencil
     st_in, st_out = s32["fields"], torch.empty_like(s32["fields"])
     V32 = s32["op"]._keep["V"]
-    ts = timed(lambda: stencil(st_in, h, "dirichlet", 4, -0.5 / h ** 2, V=V32, out=st_out), max(3, args.steps), 2)
+    from gato_gb300.autotune import tune_stencil
+    st_step = lambda: stencil(st_in, h, "dirichlet", 4, -0.5 / h ** 2, V=V32, out=st_out)  # noqa: E731
+    st_best = tune_stencil(st_step, key="bench")
+    ts = timed(st_step, max(3, args.steps), 2)
     ts_avg = sum(ts) / len(ts)
     bytes_s = 3 * n3 * 4 * N_OCC
+
+    # ---- cuFFT comparator ----------------------------------------------------------
+    cufft = cufft_comparator(s32, N, h, eps, timed, max(3, args.steps))
 
     # ---- e2e: public API with host buffers ---------------------------------------
     host_in = torch.tensor(orbs, dtype=torch.float32).pin_memory()
@@ -342,10 +399,13 @@ def run_gato(args):
                      "frac": bytes_x / tx_avg / 1e9 / peak,
                      "traffic": FMI_TRAFFIC_128 if N == 128 else None, "peak_kind": peak_kind,
                      "algorithmic_bytes": bytes_x, "avg_launch_us": tx_avg * 1e6,
-                     "limiter": "instruction issue (77% issue active, FMA pipe 55%, ncu)"},
+                     "limiter": "instruction issue (75% issue active, FMA pipe 56%, ncu)"},
         "roofline_stencil": {"bound": "hbm", "achieved": bytes_s / ts_avg / 1e9, "peak": peak, "unit": "GB/s",
-                             "frac": bytes_s / ts_avg / 1e9 / peak, "avg_launch_us": ts_avg * 1e6},
+                             "frac": bytes_s / ts_avg / 1e9 / peak, "avg_launch_us": ts_avg * 1e6,
+                             "rows_per_thread": st_best["rows"],
+                             "candidates_ms": {str(c["rows"]): round(c["ms"], 5) for c in st_best["candidates"]}},
         "cpu_baseline": cpu,
+        "cufft_comparator": dict(cufft, gato_block_apply_us=1e6 * t_max / args.steps),
         "fp64_block_applies_per_s": rate64,
         "speedup_mixed_vs_fp64": value / world / rate64,
         "matvec_applies_per_s": {"mixed": args.steps / sum(tm32), "fp64": k64 / sum(tm64)},

@@ -40,6 +40,7 @@ _SIGS = {
     "gato_dot_noalloc": [i32, vp, vp, i64, f64, vp, vp],
     "gato_normalize": [i32, vp, i64, vp, vp],
     "gato_stencil_apply": [i32, vp, vp, vp, i32, i32, i32, i32, f64, i32, i32, vp, f64, vp],
+    "gato_stencil_tune": [i32],
     "gato_softened_coulomb": [i32, vp, i32, f64, i32, P_f64, P_f64, f64, vp],
     "gato_hgh_local": [i32, vp, i32, f64, i32, P_f64, P_f64, P_f64, P_f64, vp],
     "gato_nonlocal_create": [i32, i32, f64, i32, P_f64, P_i32, P_i32, P_f64, P_i32, P_f64, f64,

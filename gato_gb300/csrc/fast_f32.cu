@@ -15,6 +15,14 @@ using T = float;
 using T2 = typename Cplx<T>::type;
 constexpr bool kF32 = sizeof(T) == 4;
 
+int shape_r2(int M) {
+#define X(MM, A, B, L32, L64) \
+  case MM: return B;
+  switch (M) { GATO_FAST_SHAPES(X) }
+#undef X
+  return 0;
+}
+
 template <>
 int rows_L<T>(int M) {
 #define X(MM, A, B, L32, L64) \

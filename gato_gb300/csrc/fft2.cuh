@@ -157,12 +157,46 @@ template <int R1, int R2> struct Shape {
   static constexpr int RMAX = R1 > R2 ? R1 : R2;
 };
 
-// Runtime twiddle W_M^{DIR * e} from the shared table tw[e] = exp(-2 pi i e / M).
+// Row stride, in entries, of the stage-twiddle table
+// tw[k1 * stride + n2] = exp(-2 pi i n2 k1 / M) (R1 rows). Consecutive lanes
+// of the row passes read consecutive rows: the padding puts those rows in
+// distinct shared-memory banks (FP32 twiddles move in 16-byte pairs, so a row
+// starts on a 16-byte boundary; FP64 twiddles are one 16-byte load each).
+__host__ __device__ constexpr int tw_row_stride(bool f32, int R2) {
+  return f32 ? ((R2 / 2) % 2 == 0 ? R2 + 2 : R2) : R2 + 1;
+}
+template <typename T2, int R2> struct TwRow {
+  static constexpr int S = tw_row_stride(sizeof(T2) == 8, R2);
+};
+
+// a * w for w = (c, s) = exp(-2 pi i e / M) (DIR = -1) or its conjugate (DIR = +1).
 template <typename T2, int DIR>
-__device__ __forceinline__ T2 rtw(T2 a, const T2* tw, int e) {
-  T2 w = tw[e];
-  if (DIR > 0) w.y = -w.y;
+__device__ __forceinline__ T2 rtw(T2 a, typename CT<T2>::R c, typename CT<T2>::R s) {
+  T2 w;
+  w.x = c;
+  w.y = DIR > 0 ? -s : s;
   return cmul(a, w);
+}
+
+// X[n2] *= W_M^{DIR n2 k1} for n2 = 1 .. R2-1 from row k1 of the stage table,
+// row[n2] = exp(-2 pi i n2 k1 / M). The row is contiguous, so float twiddles
+// come in pairs from one 16-byte shared load (R2 is even and every row starts
+// on a 16-byte boundary); n2 = 0 is the identity and skipped.
+template <typename T2, int R2, int DIR>
+__device__ __forceinline__ void twiddle_row(T2* X, const T2* row) {
+  if constexpr (sizeof(T2) == 8) {
+    static_assert(R2 % 2 == 0, "paired twiddle loads need an even R2");
+    const float4* r4 = reinterpret_cast<const float4*>(row);
+#pragma unroll
+    for (int p = 0; p < R2 / 2; ++p) {
+      const float4 w = r4[p];
+      if (p > 0) X[2 * p] = rtw<T2, DIR>(X[2 * p], w.x, w.y);
+      X[2 * p + 1] = rtw<T2, DIR>(X[2 * p + 1], w.z, w.w);
+    }
+  } else {
+#pragma unroll
+    for (int n2 = 1; n2 < R2; ++n2) X[n2] = rtw<T2, DIR>(X[n2], row[n2].x, row[n2].y);
+  }
 }
 
 // Stage 1 of the forward transform for the item (line, n2): reads x[R2 n1 + n2]
@@ -182,11 +216,13 @@ __device__ __forceinline__ void fwd_stage1(T2* buf, int LP, int line, int n2, Ge
 }
 
 // Stage 2 of the forward transform for (line, k1): X[k2] = spectrum at k1 + R1 k2.
+// tw is the stage-twiddle table (R1 rows, see tw_row_stride).
 template <typename T2, int R1, int R2>
 __device__ __forceinline__ void fwd_stage2(const T2* buf, int LP, int line, int k1, const T2* tw,
                                            T2* X) {
 #pragma unroll
-  for (int n2 = 0; n2 < R2; ++n2) X[n2] = rtw<T2, -1>(buf[(n2 * R1 + k1) * LP + line], tw, n2 * k1);
+  for (int n2 = 0; n2 < R2; ++n2) X[n2] = buf[(n2 * R1 + k1) * LP + line];
+  twiddle_row<T2, R2, -1>(X, tw + k1 * TwRow<T2, R2>::S);
   rdft<T2, R2, -1>(X);
 }
 
@@ -194,8 +230,9 @@ __device__ __forceinline__ void fwd_stage2(const T2* buf, int LP, int line, int 
 template <typename T2, int R1, int R2>
 __device__ __forceinline__ void inv_stageA(T2* buf, int LP, int line, int k1, const T2* tw, T2* X) {
   rdft<T2, R2, +1>(X);
+  twiddle_row<T2, R2, +1>(X, tw + k1 * TwRow<T2, R2>::S);
 #pragma unroll
-  for (int n2 = 0; n2 < R2; ++n2) buf[(n2 * R1 + k1) * LP + line] = rtw<T2, +1>(X[n2], tw, n2 * k1);
+  for (int n2 = 0; n2 < R2; ++n2) buf[(n2 * R1 + k1) * LP + line] = X[n2];
 }
 
 // Inverse stage B for (line, n2): outputs x[n2 + R2 n1] through `put` (n1 < R1/2 when HALF).
@@ -208,6 +245,61 @@ __device__ __forceinline__ void inv_stageB(const T2* buf, int LP, int line, int 
 #pragma unroll
   for (int n1 = 0; n1 < R1; ++n1)
     if (!HALF || n1 < R1 / 2) put(n2 + R2 * n1, w[n1]);
+}
+
+// ---- row passes (the contiguous z axis) ----------------------------------------
+// Line `line`'s stage element (n2, k1) sits at line * LS + n2 * (R1 + 1) + k1.
+// Stages 1 and B run with n2 across the lanes, stages 2 and A with k1 across
+// the lanes: both orders walk the buffer with odd element strides (no bank
+// conflicts), stage 2 leaves spectrum entries k1 + R1 k2 that consecutive
+// lanes store to consecutive addresses, and stage B leaves outputs
+// n2 + R2 n1 in the same coalesced order, so no transpose through shared
+// memory is needed on either side.
+template <int R1, int R2> struct RowBuf {
+  static constexpr int LS = R2 * (R1 + 1);
+  static __device__ __forceinline__ int at(int line, int n2, int k1) {
+    return line * LS + n2 * (R1 + 1) + k1;
+  }
+};
+
+// Stage 1 for (line, n2): v[n1] = x[R2 n1 + n2] (n1 < R1/2 only when HALF).
+template <typename T2, int R1, int R2, bool HALF>
+__device__ __forceinline__ void row_fwd_stage1(T2* buf, int line, int n2, T2* v) {
+  if constexpr (HALF) {
+#pragma unroll
+    for (int n1 = R1 / 2; n1 < R1; ++n1) v[n1].x = v[n1].y = 0;
+    rdft_half<T2, R1, -1>(v);
+  } else {
+    rdft<T2, R1, -1>(v);
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < R1; ++k1) buf[RowBuf<R1, R2>::at(line, n2, k1)] = v[k1];
+}
+
+// Stage 2 for (line, k1): X[k2] = spectrum at k1 + R1 k2.
+template <typename T2, int R1, int R2>
+__device__ __forceinline__ void row_fwd_stage2(const T2* buf, int line, int k1, const T2* tw, T2* X) {
+#pragma unroll
+  for (int n2 = 0; n2 < R2; ++n2) X[n2] = buf[RowBuf<R1, R2>::at(line, n2, k1)];
+  twiddle_row<T2, R2, -1>(X, tw + k1 * TwRow<T2, R2>::S);
+  rdft<T2, R2, -1>(X);
+}
+
+// Inverse stage A for (line, k1) holding X[k2] = spectrum at k1 + R1 k2.
+template <typename T2, int R1, int R2>
+__device__ __forceinline__ void row_inv_stageA(T2* buf, int line, int k1, const T2* tw, T2* X) {
+  rdft<T2, R2, +1>(X);
+  twiddle_row<T2, R2, +1>(X, tw + k1 * TwRow<T2, R2>::S);
+#pragma unroll
+  for (int n2 = 0; n2 < R2; ++n2) buf[RowBuf<R1, R2>::at(line, n2, k1)] = X[n2];
+}
+
+// Inverse stage B for (line, n2): w[n1] = output at z = n2 + R2 n1.
+template <typename T2, int R1, int R2>
+__device__ __forceinline__ void row_inv_stageB(const T2* buf, int line, int n2, T2* w) {
+#pragma unroll
+  for (int k1 = 0; k1 < R1; ++k1) w[k1] = buf[RowBuf<R1, R2>::at(line, n2, k1)];
+  rdft<T2, R1, +1>(w);
 }
 
 }  // namespace fft2

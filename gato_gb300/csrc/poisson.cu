@@ -22,6 +22,7 @@
 #include <cmath>
 #include <vector>
 
+#include "fft2.cuh"
 #include "poisson.cuh"
 
 namespace gato {
@@ -292,6 +293,7 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
   const int N = pl.N, M = pl.M;
   const int64_t nrows = (int64_t)N * N;
   const T2* tw = (const T2*)pl.tw;
+  const T2* tw2 = (const T2*)pl.tw2;   // the register engine's per-row stage twiddles
   T2* S1 = (T2*)pl.S1;
   T2* S2 = (T2*)pl.S2;
   const int Lf = pl.engine == 0 ? fast::rows_L<T>(M) : 0;   // register engine, 0: generic
@@ -321,14 +323,14 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
     const int64_t sstride = (int64_t)ngroups * nblk_i;
     if (Lf > 0) {
       // register-resident two-pass engine
-      GATO_TRY(fast::rows_fwd<T>(M, args, f0, nfg, S1, tw, s));
-      GATO_TRY(fast::cols<T>(M, COL_FWD, S1, S2, gy, N, nfg, tw, nullptr, pl.H, s));
-      GATO_TRY(fast::cols<T>(M, COL_FMI, S2, S2, gx, M, nfg, tw, (const T*)pl.ghat, pl.H, s));
-      GATO_TRY(fast::cols<T>(M, COL_INV, S2, S1, gyi, N, nfg, tw, nullptr, pl.H, s));
+      GATO_TRY(fast::rows_fwd<T>(M, args, f0, nfg, S1, tw2, s));
+      GATO_TRY(fast::cols<T>(M, COL_FWD, S1, S2, gy, N, nfg, tw2, nullptr, pl.H, s));
+      GATO_TRY(fast::cols<T>(M, COL_FMI, S2, S2, gx, M, nfg, tw2, (const T*)pl.ghat, pl.H, s));
+      GATO_TRY(fast::cols<T>(M, COL_INV, S2, S1, gyi, N, nfg, tw2, nullptr, pl.H, s));
       if (epi == EPI_J)
-        GATO_TRY(fast::rows_inv_j<T>(M, args, f0, nfg, S1, tw, s));
+        GATO_TRY(fast::rows_inv_j<T>(M, args, f0, nfg, S1, tw2, s));
       else
-        GATO_TRY(fast::rows_inv<T>(M, args, f0, nfg, S1, tw, acc_here ? 1 : 0, epi == EPI_ENERGY, part,
+        GATO_TRY(fast::rows_inv<T>(M, args, f0, nfg, S1, tw2, acc_here ? 1 : 0, epi == EPI_ENERGY, part,
                                    sstride, s));
       continue;
     }
@@ -397,6 +399,24 @@ static int plan_create(int dtype, int N, double h, double eps, int max_fields, P
   GATO_CUDA_TRY(cudaMalloc(&pl.tw, (size_t)M * 2 * ts));
   GATO_CUDA_TRY(cudaMemcpy(pl.tw, dtype == GATO_F64 ? (void*)tw64.data() : (void*)tw32.data(),
                            (size_t)M * 2 * ts, cudaMemcpyHostToDevice));
+  if (const int R2 = fast::shape_r2(M)) {
+    // the register engine's stage twiddles: row k1 holds exp(-2 pi i n2 k1 / M)
+    // for n2 < R2, rows padded to the stride the kernels read them with
+    const int R1 = M / R2;
+    const int S = fft2::tw_row_stride(dtype == GATO_F32, R2);
+    std::vector<double2> t64((size_t)R1 * S, make_double2(0.0, 0.0));
+    std::vector<float2> t32((size_t)R1 * S, make_float2(0.f, 0.f));
+    for (int k1 = 0; k1 < R1; ++k1)
+      for (int n2 = 0; n2 < R2; ++n2) {
+        const double2 w = tw64[(size_t)n2 * k1];   // n2 k1 < M
+        t64[(size_t)k1 * S + n2] = w;
+        t32[(size_t)k1 * S + n2] = make_float2((float)w.x, (float)w.y);
+      }
+    const size_t bytes = (size_t)R1 * S * 2 * ts;
+    GATO_CUDA_TRY(cudaMalloc(&pl.tw2, bytes));
+    GATO_CUDA_TRY(cudaMemcpy(pl.tw2, dtype == GATO_F64 ? (void*)t64.data() : (void*)t32.data(), bytes,
+                             cudaMemcpyHostToDevice));
+  }
   double2* tw_d = nullptr;
   GATO_CUDA_TRY(cudaMalloc(&tw_d, (size_t)M * sizeof(double2)));
   GATO_CUDA_TRY(cudaMemcpy(tw_d, tw64.data(), (size_t)M * sizeof(double2), cudaMemcpyHostToDevice));
@@ -436,7 +456,7 @@ static int plan_create(int dtype, int N, double h, double eps, int max_fields, P
 }
 
 static void plan_free(PoissonPlan& pl) {
-  free_after_pending({pl.ghat, pl.tw, pl.S1, pl.S2, pl.partials});
+  free_after_pending({pl.ghat, pl.tw, pl.tw2, pl.S1, pl.S2, pl.partials});
   pl = PoissonPlan{};
 }
 
@@ -539,7 +559,7 @@ extern "C" int gato_poisson_stage(gato_poisson_t plan, int stage, int nf, void* 
   const int N = pl.N, M = pl.M;
   const int64_t nrows = (int64_t)N * N;
   cudaStream_t s = as_stream(stream);
-  auto run = [&](auto* S1, auto* S2, auto* tw, auto* ghat) -> int {
+  auto run = [&](auto* S1, auto* S2, auto* tw, auto* tw2, auto* ghat) -> int {
     using T2 = std::remove_pointer_t<decltype(S1)>;
     using T = std::remove_const_t<std::remove_pointer_t<decltype(ghat)>>;
     const int mode = stage == 1 ? COL_FWD : (stage == 2 ? COL_FMI : COL_INV);
@@ -548,7 +568,7 @@ extern "C" int gato_poisson_stage(gato_poisson_t plan, int stage, int nf, void* 
       ColGeom g2{(int64_t)N * M * M, (int64_t)N * M * M, M, M, (int64_t)M * M, (int64_t)M * M, M, N, N};
       ColGeom g3{(int64_t)N * M * M, nrows * M, (int64_t)M * M, (int64_t)N * M, M, M, M, M, N};
       return fast::cols<T>(M, mode, stage == 1 ? S1 : S2, stage == 3 ? S1 : S2,
-                           stage == 1 ? g1 : (stage == 2 ? g2 : g3), stage == 2 ? M : N, nf, tw,
+                           stage == 1 ? g1 : (stage == 2 ? g2 : g3), stage == 2 ? M : N, nf, tw2,
                            stage == 2 ? ghat : nullptr, pl.H, s);
     }
     if (stage == 1) {
@@ -563,8 +583,9 @@ extern "C" int gato_poisson_stage(gato_poisson_t plan, int stage, int nf, void* 
     return launch_cols<T2>(COL_INV, S2, S1, g, N, nf, pl.fp, tw, nullptr, pl.H, s);
   };
   if (pl.dtype == GATO_F64)
-    return run((double2*)pl.S1, (double2*)pl.S2, (const double2*)pl.tw, (const double*)pl.ghat);
-  return run((float2*)pl.S1, (float2*)pl.S2, (const float2*)pl.tw, (const float*)pl.ghat);
+    return run((double2*)pl.S1, (double2*)pl.S2, (const double2*)pl.tw, (const double2*)pl.tw2,
+               (const double*)pl.ghat);
+  return run((float2*)pl.S1, (float2*)pl.S2, (const float2*)pl.tw, (const float2*)pl.tw2, (const float*)pl.ghat);
 }
 
 // Tuning knobs: fields per launch group (1..max_fields, 0 = all) and the FFT

@@ -43,6 +43,8 @@ struct PoissonPlan {
   FftPlanDev fp{};
   void* ghat = nullptr;    // H^3 octant of the kernel spectrum, x dV / M^3
   void* tw = nullptr;      // M twiddles exp(-2 pi i k / M)
+  void* tw2 = nullptr;     // register engine: tw2[k1 S + n2] = exp(-2 pi i n2 k1 / M), M = R1 R2,
+                           // S = fft2::tw_row_stride
   void* S1 = nullptr;      // max_fields x N x N x M complex
   void* S2 = nullptr;      // max_fields x N x M x M complex
   double* partials = nullptr;
@@ -76,6 +78,7 @@ __device__ __forceinline__ T dens(const PartDesc& d, const void* const* in, int6
 namespace fast {
 constexpr int kNotHandled = 1;
 template <typename T> int rows_L(int M);   // lines per CTA of the z kernels, 0 if unsupported
+int shape_r2(int M);                        // R2 of the register engine's M = R1 R2, 0 if none
 template <typename T>
 int cols(int M, int mode, const typename Cplx<T>::type* in, typename Cplx<T>::type* out,
          const ColGeom& g, int outer, int nf, const typename Cplx<T>::type* tw, const T* ghat,

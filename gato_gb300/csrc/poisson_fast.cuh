@@ -10,25 +10,25 @@ namespace fast {
 using namespace fft2;
 
 
-// The M-entry twiddle table split into a register prefetch at kernel entry
-// and a shared-memory store placed after the kernel's own field loads are
-// issued, so the two global latencies overlap instead of adding up.
-template <typename T2, int M, int NT>
+// The COUNT-entry stage-twiddle table split into a register prefetch at
+// kernel entry and a shared-memory store placed after the kernel's own field
+// loads are issued, so the two global latencies overlap instead of adding up.
+template <typename T2, int COUNT, int NT>
 struct TwPrefetch {
-  static constexpr int K = (M + NT - 1) / NT;
+  static constexpr int K = (COUNT + NT - 1) / NT;
   T2 v[K];
   __device__ __forceinline__ explicit TwPrefetch(const T2* tw) {
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       const int i = threadIdx.x + k * NT;
-      if (i < M) v[k] = tw[i];
+      if (i < COUNT) v[k] = tw[i];
     }
   }
   __device__ __forceinline__ void store(T2* tws) const {
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       const int i = threadIdx.x + k * NT;
-      if (i < M) tws[i] = v[k];
+      if (i < COUNT) tws[i] = v[k];
     }
   }
 };
@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   extern __shared__ __align__(16) unsigned char smraw[];
   T2* buf = reinterpret_cast<T2*>(smraw);
   T2* tws = buf + M * LP;
-  const TwPrefetch<T2, M, L * Shape<R1, R2>::RMAX> twp(tw);
+  const TwPrefetch<T2, R1 * TwRow<T2, R2>::S, L * Shape<R1, R2>::RMAX> twp(tw);
   const int outer = blockIdx.x, col0 = blockIdx.y * L, f = blockIdx.z;
   const int t = threadIdx.x;
   const int line = t % L, q = t / L;   // q: n2 in stages 1/B, k1 in stages 2/A
@@ -114,80 +114,63 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   }
 }
 
-// z forward with the pair-density prologue. One shared buffer: each thread
-// holds its stage inputs in registers across the barrier that separates the
-// reads of one stage from the writes of the next.
+// ---- z passes (rows) ---------------------------------------------------------------
+// A CTA owns L consecutive rows (x, y) of the z axis; thread t works on line
+// t / RMAX as item j = t % RMAX: n2 in stages 1 and B, k1 in stages 2 and A
+// (the RowBuf layout of fft2.cuh). Field rows are read and spectra written
+// straight from registers with lanes on consecutive z (or kz), so every
+// global access is coalesced and no shared-memory transpose is needed.
+
+// Pair density of part q of a field at element gi (0 when the part is absent).
+template <typename T>
+__device__ __forceinline__ T part_density(const T* a, const T* b, int64_t gi) {
+  if (!a) return (T)0;
+  T v = a[gi];
+  if (b) v *= b[gi];
+  return v;
+}
+
+// z forward with the pair-density prologue, one field per CTA (grid.y = field).
 template <typename T, int R1, int R2, int L>
 __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
     k_rows_fwd(PassArgs args, int f0, typename Cplx<T>::type* S1, const typename Cplx<T>::type* tw) {
   using T2 = typename Cplx<T>::type;
-  constexpr int M = R1 * R2, N = M / 2, LP = L + 1;
+  constexpr int M = R1 * R2, N = M / 2, RM = Shape<R1, R2>::RMAX, NT = L * RM;
   extern __shared__ __align__(16) unsigned char smraw[];
   T2* buf = reinterpret_cast<T2*>(smraw);
-  T2* tws = buf + M * LP;
-  constexpr int NT = L * Shape<R1, R2>::RMAX;
-  const TwPrefetch<T2, M, NT> twp(tw);
-  constexpr int EIN = (L * N + NT - 1) / NT;   // input elements per thread
-  constexpr int EOUT = (L * M + NT - 1) / NT;  // output elements per thread
+  T2* tws = buf + L * RowBuf<R1, R2>::LS;
+  const TwPrefetch<T2, R1 * TwRow<T2, R2>::S, NT> twp(tw);
   const int p = blockIdx.y;
   const FieldDesc& fd = args.f[f0 + p];
-  const int64_t row0 = (int64_t)blockIdx.x * L;
   const int64_t nrows = (int64_t)N * N;
+  const int line = threadIdx.x / RM, j = threadIdx.x % RM;
+  const int64_t r = (int64_t)blockIdx.x * L + line;
+  const bool live = r < nrows;
   // the pair-density factors of the real and imaginary parts (null: factor absent)
   const T* a0 = reinterpret_cast<const T*>(args.in[fd.p[0].a]);
   const T* b0 = fd.p[0].b >= 0 ? reinterpret_cast<const T*>(args.in[fd.p[0].b]) : nullptr;
   const T* a1 = fd.p[1].a >= 0 ? reinterpret_cast<const T*>(args.in[fd.p[1].a]) : nullptr;
   const T* b1 = (a1 && fd.p[1].b >= 0) ? reinterpret_cast<const T*>(args.in[fd.p[1].b]) : nullptr;
-  // every load of this thread is issued before the first shared-memory store
-  T2 vin[EIN];
+  T2 v[R1];
+  if (j < R2) {
 #pragma unroll
-  for (int e = 0; e < EIN; ++e) {
-    const int i = threadIdx.x + e * NT;
-    const int64_t r = row0 + i / N;
-    vin[e].x = vin[e].y = 0;
-    if (i < L * N && r < nrows) {
-      const int64_t gi = r * N + i % N;
-      vin[e].x = a0[gi];
-      if (b0) vin[e].x *= b0[gi];
-      if (a1) {
-        vin[e].y = a1[gi];
-        if (b1) vin[e].y *= b1[gi];
-      }
+    for (int n1 = 0; n1 < R1 / 2; ++n1) {
+      const int64_t gi = r * N + R2 * n1 + j;
+      v[n1].x = live ? part_density(a0, b0, gi) : (T)0;
+      v[n1].y = live ? part_density(a1, b1, gi) : (T)0;
     }
   }
   twp.store(tws);
-#pragma unroll
-  for (int e = 0; e < EIN; ++e) {
-    const int i = threadIdx.x + e * NT;
-    if (i < L * N) buf[(i % N) * LP + i / N] = vin[e];
-  }
+  if (j < R2) row_fwd_stage1<T2, R1, R2, true>(buf, line, j, v);
   __syncthreads();
-  const int t = threadIdx.x, line = t % L, q = t / L;
-  T2 v[R1];
-  if (q < R2) {
+  if (j < R1) {
+    T2 X[R2];
+    row_fwd_stage2<T2, R1, R2>(buf, line, j, tws, X);
+    if (live) {
+      T2* d = S1 + (int64_t)p * nrows * M + r * M + j;
 #pragma unroll
-    for (int n1 = 0; n1 < R1 / 2; ++n1) v[n1] = buf[(R2 * n1 + q) * LP + line];
-    rdft_half<T2, R1, -1>(v);
-  }
-  __syncthreads();
-  if (q < R2)
-#pragma unroll
-    for (int k1 = 0; k1 < R1; ++k1) buf[(q * R1 + k1) * LP + line] = v[k1];
-  __syncthreads();
-  T2 X[R2];
-  if (q < R1) fwd_stage2<T2, R1, R2>(buf, LP, line, q, tws, X);
-  __syncthreads();
-  if (q < R1)
-#pragma unroll
-    for (int k2 = 0; k2 < R2; ++k2) buf[(q + R1 * k2) * LP + line] = X[k2];
-  __syncthreads();
-  T2* dst = S1 + (int64_t)p * nrows * M;
-#pragma unroll
-  for (int e = 0; e < EOUT; ++e) {
-    const int i = threadIdx.x + e * NT;
-    const int ln = i / M, kz = i % M;
-    const int64_t r = row0 + ln;
-    if (i < L * M && r < nrows) dst[r * M + kz] = buf[kz * LP + ln];
+      for (int k2 = 0; k2 < R2; ++k2) d[R1 * k2] = X[k2];
+    }
   }
 }
 
@@ -203,21 +186,18 @@ struct RowsIn {
 // input (the orbitals, psi) are staged in shared memory once, then each field's
 // pair densities are formed straight into the stage-1 registers of its FFT.
 // Same transform and output as k_rows_fwd, without re-reading the inputs per
-// field. Staged rows are padded to N + 1 so the 16 lines a warp reads in stage 1
-// fall in different banks.
+// field. Staged rows are padded to N + 1; stage-1 lanes read consecutive z.
 template <typename T, int R1, int R2, int L>
 __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
     k_rows_fwd_multi(PassArgs args, RowsIn ri, int f0, int nfg, typename Cplx<T>::type* S1,
                      const typename Cplx<T>::type* tw) {
   using T2 = typename Cplx<T>::type;
-  constexpr int M = R1 * R2, N = M / 2, LP = L + 1, NP = N + 1;
-  constexpr int NT = L * Shape<R1, R2>::RMAX;
-  constexpr int EOUT = (L * M + NT - 1) / NT;
+  constexpr int M = R1 * R2, N = M / 2, NP = N + 1, RM = Shape<R1, R2>::RMAX, NT = L * RM;
   extern __shared__ __align__(16) unsigned char smraw[];
   T2* buf = reinterpret_cast<T2*>(smraw);
-  T2* tws = buf + M * LP;
-  T* stage = reinterpret_cast<T*>(tws + M);   // [slot][line][z], rows of NP
-  const TwPrefetch<T2, M, NT> twp(tw);
+  T2* tws = buf + L * RowBuf<R1, R2>::LS;
+  T* stage = reinterpret_cast<T*>(tws + R1 * TwRow<T2, R2>::S);   // [slot][line][z], rows of NP
+  const TwPrefetch<T2, R1 * TwRow<T2, R2>::S, NT> twp(tw);
   const int64_t row0 = (int64_t)blockIdx.x * L;
   const int64_t nrows = (int64_t)N * N;
   // staging: 8 loads in flight per thread per batch
@@ -243,18 +223,19 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   }
   twp.store(tws);
   __syncthreads();
-  const int t = threadIdx.x, line = t % L, q = t / L;
+  const int line = threadIdx.x / RM, j = threadIdx.x % RM;
+  const int64_t r = row0 + line;
   for (int p = 0; p < nfg; ++p) {
     const FieldDesc& fd = args.f[f0 + p];
-    const int a0 = ri.slot_of[fd.p[0].a];
-    const int b0 = fd.p[0].b >= 0 ? ri.slot_of[fd.p[0].b] : -1;
-    const int a1 = fd.p[1].a >= 0 ? ri.slot_of[fd.p[1].a] : -1;
-    const int b1 = (a1 >= 0 && fd.p[1].b >= 0) ? ri.slot_of[fd.p[1].b] : -1;
-    if (q < R2) {
+    if (j < R2) {
+      const int a0 = ri.slot_of[fd.p[0].a];
+      const int b0 = fd.p[0].b >= 0 ? ri.slot_of[fd.p[0].b] : -1;
+      const int a1 = fd.p[1].a >= 0 ? ri.slot_of[fd.p[1].a] : -1;
+      const int b1 = (a1 >= 0 && fd.p[1].b >= 0) ? ri.slot_of[fd.p[1].b] : -1;
       T2 v[R1];
 #pragma unroll
       for (int n1 = 0; n1 < R1 / 2; ++n1) {
-        const int z = R2 * n1 + q;
+        const int z = R2 * n1 + j;
         T x = stage[(a0 * L + line) * NP + z];
         if (b0 >= 0) x *= stage[(b0 * L + line) * NP + z];
         T y = (T)0;
@@ -265,25 +246,17 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
         v[n1].x = x;
         v[n1].y = y;
       }
-      rdft_half<T2, R1, -1>(v);
-#pragma unroll
-      for (int k1 = 0; k1 < R1; ++k1) buf[(q * R1 + k1) * LP + line] = v[k1];
+      row_fwd_stage1<T2, R1, R2, true>(buf, line, j, v);
     }
     __syncthreads();
-    T2 X[R2];
-    if (q < R1) fwd_stage2<T2, R1, R2>(buf, LP, line, q, tws, X);
-    __syncthreads();
-    if (q < R1)
+    if (j < R1) {
+      T2 X[R2];
+      row_fwd_stage2<T2, R1, R2>(buf, line, j, tws, X);
+      if (r < nrows) {
+        T2* d = S1 + (int64_t)p * nrows * M + r * M + j;
 #pragma unroll
-      for (int k2 = 0; k2 < R2; ++k2) buf[(q + R1 * k2) * LP + line] = X[k2];
-    __syncthreads();
-    T2* dst = S1 + (int64_t)p * nrows * M;
-#pragma unroll
-    for (int e = 0; e < EOUT; ++e) {
-      const int i = threadIdx.x + e * NT;
-      const int ln = i / M, kz = i % M;
-      const int64_t r = row0 + ln;
-      if (i < L * M && r < nrows) dst[r * M + kz] = buf[kz * LP + ln];
+        for (int k2 = 0; k2 < R2; ++k2) d[R1 * k2] = X[k2];
+      }
     }
     __syncthreads();   // buf is rewritten by the next field
   }
@@ -291,34 +264,33 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
 
 // z inverse over every field of the group, then the epilogue. NO > 0: the
 // accumulation terms target outputs < NO, kept in registers (each thread owns
-// EPT fixed (row, z) elements); NO == 0: energy mode.
+// the R1/2 fixed elements z = j + R2 n1 of its row); NO == 0: energy mode.
 template <typename T, int R1, int R2, int L, int NO>
 __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
     k_rows_inv(PassArgs args, int f0, int nfg, const typename Cplx<T>::type* S1,
                const typename Cplx<T>::type* tw, int accumulate, double* partials,
                int64_t slot_stride) {
   using T2 = typename Cplx<T>::type;
-  constexpr int M = R1 * R2, N = M / 2, LP = L + 1;
-  constexpr int NT = L * Shape<R1, R2>::RMAX;
-  constexpr int EPT = (L * N + NT - 1) / NT;
+  constexpr int M = R1 * R2, N = M / 2, RM = Shape<R1, R2>::RMAX, NT = L * RM;
+  constexpr int EPT = R1 / 2;
   constexpr bool ENERGY = NO == 0;
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ double sh[32];
   T2* buf = reinterpret_cast<T2*>(smraw);
-  T2* tws = buf + M * LP;
-  const TwPrefetch<T2, M, NT> twp(tw);
-  const int64_t row0 = (int64_t)blockIdx.x * L;
+  T2* tws = buf + L * RowBuf<R1, R2>::LS;
+  const TwPrefetch<T2, R1 * TwRow<T2, R2>::S, NT> twp(tw);
   const int64_t nrows = (int64_t)N * N;
+  const int line = threadIdx.x / RM, j = threadIdx.x % RM;
+  const int64_t r = (int64_t)blockIdx.x * L + line;
+  const bool own = j < R2 && r < nrows;   // this thread owns elements of the output
   T acc[ENERGY ? 1 : NO][EPT];
 #pragma unroll
   for (int o = 0; o < (ENERGY ? 1 : NO); ++o)
 #pragma unroll
     for (int e = 0; e < EPT; ++e) acc[o][e] = (T)0;
   Acc<T> e0, e1;
-  const int t = threadIdx.x, line = t % L, q = t / L;
   for (int p = 0; p < nfg; ++p) {
     const FieldDesc& fd = args.f[f0 + p];
-    const T2* src = S1 + (int64_t)p * nrows * M;
     // The epilogue's first field factor of each part (in[tc] of term 0, or the
     // density in energy mode) does not depend on the transform: load it now so
     // its latency overlaps the FFT instead of following it. A second term
@@ -326,95 +298,59 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
     T fac[EPT][2];
 #pragma unroll
     for (int e = 0; e < EPT; ++e) {
-      const int i = e * NT + t;
-      const int64_t r = row0 + i / N;
-      const bool ok = i < L * N && r < nrows;
-      const int64_t gi = r * N + i % N;
+      const int64_t gi = r * N + j + R2 * e;
 #pragma unroll
       for (int qq = 0; qq < 2; ++qq) {
         const PartDesc& d = fd.p[qq];
         if constexpr (ENERGY)
-          fac[e][qq] = (ok && d.a >= 0) ? dens<T>(d, args.in, gi) : (T)0;
+          fac[e][qq] = (own && d.a >= 0) ? dens<T>(d, args.in, gi) : (T)0;
         else
-          fac[e][qq] = (ok && d.a >= 0 && d.nt > 0)
+          fac[e][qq] = (own && d.a >= 0 && d.nt > 0)
                            ? (d.tc[0] >= 0 ? reinterpret_cast<const T*>(args.in[d.tc[0]])[gi] : (T)1)
                            : (T)0;
       }
     }
-    // loads in batches of at most 8 elements per thread (the accumulators
-    // already hold NO x EPT registers); the first batch is in flight across
-    // the barrier that frees buf
-    constexpr int ESP = (L * M + NT - 1) / NT;
-    constexpr int CH = ESP < 8 ? ESP : 8;
-#pragma unroll
-    for (int c = 0; c < ESP; c += CH) {
-      T2 vin[CH];
-#pragma unroll
-      for (int e = 0; e < CH; ++e) {
-        const int i = threadIdx.x + (c + e) * NT;
-        const int64_t r = row0 + i / M;
-        if (c + e < ESP && i < L * M && r < nrows) vin[e] = src[r * M + i % M];
-        else vin[e].x = vin[e].y = 0;
-      }
-      if (c == 0) {
-        if (p == 0) twp.store(tws);
-        __syncthreads();
-      }
-#pragma unroll
-      for (int e = 0; e < CH; ++e) {
-        const int i = threadIdx.x + (c + e) * NT;
-        if (c + e < ESP && i < L * M) buf[(i % M) * LP + i / M] = vin[e];
-      }
-    }
-    __syncthreads();
     T2 X[R2];
-    if (q < R1) {
+    if (j < R1) {
+      const T2* src = S1 + (int64_t)p * nrows * M + r * M + j;
 #pragma unroll
-      for (int k2 = 0; k2 < R2; ++k2) X[k2] = buf[(q + R1 * k2) * LP + line];
+      for (int k2 = 0; k2 < R2; ++k2) {
+        if (r < nrows) X[k2] = src[R1 * k2];
+        else X[k2].x = X[k2].y = 0;
+      }
     }
+    if (p == 0) twp.store(tws);
+    __syncthreads();   // tws is visible; the previous field's stage-B reads of buf are done
+    if (j < R1) row_inv_stageA<T2, R1, R2>(buf, line, j, tws, X);
     __syncthreads();
-    if (q < R1) inv_stageA<T2, R1, R2>(buf, LP, line, q, tws, X);
-    __syncthreads();
-    T2 w[R1];
-    if (q < R2) {
+    if (own) {
+      T2 w[R1];
+      row_inv_stageB<T2, R1, R2>(buf, line, j, w);
 #pragma unroll
-      for (int k1 = 0; k1 < R1; ++k1) w[k1] = buf[(q * R1 + k1) * LP + line];
-      rdft<T2, R1, +1>(w);
-    }
-    __syncthreads();
-    if (q < R2)
+      for (int e = 0; e < EPT; ++e) {
+        const int64_t gi = r * N + j + R2 * e;
+        const T2 J = w[e];
 #pragma unroll
-      for (int n1 = 0; n1 < R1 / 2; ++n1) buf[(q + R2 * n1) * LP + line] = w[n1];
-    __syncthreads();
+        for (int qq = 0; qq < 2; ++qq) {
+          const PartDesc& d = fd.p[qq];
+          if (d.a < 0) continue;
+          const T val = qq == 0 ? J.x : J.y;
+          if constexpr (ENERGY) {
+            const T de = fac[e][qq];
+            if (d.eslot == 0) e0.add_prod(de * (T)d.ew, val);
+            else e1.add_prod(de * (T)d.ew, val);
+          } else {
 #pragma unroll
-    for (int e = 0; e < EPT; ++e) {
-      const int i = e * NT + t;
-      if (i >= L * N) break;
-      const int ln = i / N, z = i % N;
-      const int64_t r = row0 + ln;
-      if (r >= nrows) continue;
-      const int64_t gi = r * N + z;
-      const T2 J = buf[z * LP + ln];
+            for (int k = 0; k < 2; ++k) {
+              if (k >= d.nt) break;
+              T m = (T)d.coef[k];
+              if (k == 0) m *= fac[e][qq];
+              else if (d.tc[1] >= 0) m *= reinterpret_cast<const T*>(args.in[d.tc[1]])[gi];
+              const int to = d.to[k];
 #pragma unroll
-      for (int qq = 0; qq < 2; ++qq) {
-        const PartDesc& d = fd.p[qq];
-        if (d.a < 0) continue;
-        const T val = qq == 0 ? J.x : J.y;
-        if constexpr (ENERGY) {
-          const T de = fac[e][qq];
-          if (d.eslot == 0) e0.add_prod(de * (T)d.ew, val);
-          else e1.add_prod(de * (T)d.ew, val);
-        } else {
-#pragma unroll
-          for (int k = 0; k < 2; ++k) {
-            if (k >= d.nt) break;
-            T m = (T)d.coef[k];
-            if (k == 0) m *= fac[e][qq];
-            else if (d.tc[1] >= 0) m *= reinterpret_cast<const T*>(args.in[d.tc[1]])[gi];
-            const int to = d.to[k];
-#pragma unroll
-            for (int o = 0; o < NO; ++o)
-              if (o == to) acc[o][e] += m * val;
+              for (int o = 0; o < NO; ++o)
+                if (o == to) acc[o][e] += m * val;
+            }
           }
         }
       }
@@ -428,21 +364,14 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
       partials[slot_stride + blockIdx.x] = s1;
     }
   } else {
+    if (!own) return;
     const int nout = args.nout;
 #pragma unroll
     for (int o = 0; o < NO; ++o) {
       if (o >= nout) break;
-      T* dst = reinterpret_cast<T*>(args.out[o]);
+      T* dst = reinterpret_cast<T*>(args.out[o]) + r * N + j;
 #pragma unroll
-      for (int e = 0; e < EPT; ++e) {
-        const int i = e * NT + t;
-        if (i >= L * N) break;
-        const int ln = i / N, z = i % N;
-        const int64_t r = row0 + ln;
-        if (r >= nrows) continue;
-        const int64_t gi = r * N + z;
-        dst[gi] = accumulate ? dst[gi] + acc[o][e] : acc[o][e];
-      }
+      for (int e = 0; e < EPT; ++e) dst[R2 * e] = accumulate ? dst[R2 * e] + acc[o][e] : acc[o][e];
     }
   }
 }
@@ -454,66 +383,38 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
     k_rows_inv_j(T* jbase, int64_t jstride, int f0, const typename Cplx<T>::type* S1,
                  const typename Cplx<T>::type* tw) {
   using T2 = typename Cplx<T>::type;
-  constexpr int M = R1 * R2, N = M / 2, LP = L + 1;
+  constexpr int M = R1 * R2, N = M / 2, RM = Shape<R1, R2>::RMAX, NT = L * RM;
   extern __shared__ __align__(16) unsigned char smraw[];
   T2* buf = reinterpret_cast<T2*>(smraw);
-  T2* tws = buf + M * LP;
-  constexpr int NT = L * Shape<R1, R2>::RMAX;
-  const TwPrefetch<T2, M, NT> twp(tw);
+  T2* tws = buf + L * RowBuf<R1, R2>::LS;
+  const TwPrefetch<T2, R1 * TwRow<T2, R2>::S, NT> twp(tw);
   const int p = blockIdx.y;
-  const int64_t row0 = (int64_t)blockIdx.x * L;
   const int64_t nrows = (int64_t)N * N;
-  const T2* src = S1 + (int64_t)p * nrows * M;
-  constexpr int ESP = (L * M + NT - 1) / NT;
-  {
-    T2 vin[ESP];
-#pragma unroll
-    for (int e = 0; e < ESP; ++e) {
-      const int i = threadIdx.x + e * NT;
-      const int64_t r = row0 + i / M;
-      if (i < L * M && r < nrows) vin[e] = src[r * M + i % M];
-      else vin[e].x = vin[e].y = 0;
-    }
-    twp.store(tws);
-#pragma unroll
-    for (int e = 0; e < ESP; ++e) {
-      const int i = threadIdx.x + e * NT;
-      if (i < L * M) buf[(i % M) * LP + i / M] = vin[e];
-    }
-  }
-  __syncthreads();
-  const int t = threadIdx.x, line = t % L, q = t / L;
+  const int line = threadIdx.x / RM, j = threadIdx.x % RM;
+  const int64_t r = (int64_t)blockIdx.x * L + line;
   T2 X[R2];
-  if (q < R1) {
+  if (j < R1) {
+    const T2* src = S1 + (int64_t)p * nrows * M + r * M + j;
 #pragma unroll
-    for (int k2 = 0; k2 < R2; ++k2) X[k2] = buf[(q + R1 * k2) * LP + line];
+    for (int k2 = 0; k2 < R2; ++k2) {
+      if (r < nrows) X[k2] = src[R1 * k2];
+      else X[k2].x = X[k2].y = 0;
+    }
   }
+  twp.store(tws);
   __syncthreads();
-  if (q < R1) inv_stageA<T2, R1, R2>(buf, LP, line, q, tws, X);
+  if (j < R1) row_inv_stageA<T2, R1, R2>(buf, line, j, tws, X);
   __syncthreads();
-  T2 w[R1];
-  if (q < R2) {
+  if (j < R2 && r < nrows) {
+    T2 w[R1];
+    row_inv_stageB<T2, R1, R2>(buf, line, j, w);
+    T* jre = jbase + (int64_t)(2 * (f0 + p)) * jstride + r * N + j;
+    T* jim = jre + jstride;
 #pragma unroll
-    for (int k1 = 0; k1 < R1; ++k1) w[k1] = buf[(q * R1 + k1) * LP + line];
-    rdft<T2, R1, +1>(w);
-  }
-  __syncthreads();
-  if (q < R2)
-#pragma unroll
-    for (int n1 = 0; n1 < R1 / 2; ++n1) buf[(q + R2 * n1) * LP + line] = w[n1];
-  __syncthreads();
-  T* jre = jbase + (int64_t)(2 * (f0 + p)) * jstride;
-  T* jim = jre + jstride;
-  constexpr int EJ = (L * N + NT - 1) / NT;
-#pragma unroll
-  for (int e = 0; e < EJ; ++e) {
-    const int i = threadIdx.x + e * NT;
-    const int ln = i / N, z = i % N;
-    const int64_t r = row0 + ln;
-    if (i >= L * N || r >= nrows) continue;
-    const T2 J = buf[z * LP + ln];
-    jre[r * N + z] = J.x;
-    jim[r * N + z] = J.y;
+    for (int n1 = 0; n1 < R1 / 2; ++n1) {
+      jre[R2 * n1] = w[n1].x;
+      jim[R2 * n1] = w[n1].y;
+    }
   }
 }
 
@@ -528,8 +429,9 @@ template <typename T, int R1, int R2, int L>
 struct Launch {
   using T2 = typename Cplx<T>::type;
   static constexpr int M = R1 * R2, N = M / 2, NT = L * Shape<R1, R2>::RMAX;
-  static size_t sm_cols() { return (size_t)(M * (L + 1) + M) * sizeof(T2); }
-  static size_t sm_rows() { return (size_t)(M * (L + 1) + M) * sizeof(T2); }
+  static constexpr int TWN = R1 * TwRow<T2, R2>::S;   // stage-twiddle table entries
+  static size_t sm_cols() { return (size_t)(M * (L + 1) + TWN) * sizeof(T2); }
+  static size_t sm_rows() { return (size_t)(L * RowBuf<R1, R2>::LS + TWN) * sizeof(T2); }
   static int cols(int mode, const T2* in, T2* out, const ColGeom& g, int outer, int nf, const T2* tw,
                   const T* ghat, int H, cudaStream_t s) {
     if (g.ncols % L == 0) return cols_t<true>(mode, in, out, g, outer, nf, tw, ghat, H, s);

@@ -3,21 +3,23 @@
 //
 // Hot path (Dirichlet, 16-byte aligned rows): each CTA owns a 32 (y) x 32 (z)
 // column of the grid and marches along x through a chunk of planes. One
-// elected thread streams (16+2R) x (32+2A) halo planes into an 8-slot
+// elected thread streams (32+2R) x (32+2A) halo planes into a 6-slot
 // shared-memory ring with TMA (cp.async.bulk.tensor, mbarrier completion);
 // the tensor map's zero out-of-bounds fill is exactly the reference's zero
-// padding, so no boundary branches exist. x-neighbours live in a per-thread
-// register queue, y/z neighbours are read from the centre plane in shared
-// memory. The 16 x 32 V tile of each centre plane rides in the same ring slot
-// (a second tensor map, same mbarrier), so V arrives with the ring's
-// look-ahead instead of one DRAM round trip per plane; the output is a plain
-// coalesced store. HBM-bound: the algorithmic traffic is 3 N^3 s bytes
-// (psi, V, out).
+// padding, so no boundary branches exist. Each thread owns a z pair of 4 (or
+// 2) rows: x-neighbours live in a per-thread register queue, y/z neighbours
+// are pair reads of the centre plane in shared memory. The 32 x 32 V tile of
+// each centre plane rides in the same ring slot (a second tensor map, same
+// mbarrier), so V arrives with the ring's look-ahead instead of one DRAM
+// round trip per plane; the output is a coalesced pair store. HBM-bound: the
+// algorithmic traffic is 3 N^3 s bytes (psi, V, out).
 #include <cuda.h>
 
 #include <algorithm>
 #include <atomic>
 #include <cstring>
+#include <type_traits>
+#include <utility>
 
 #include "common.cuh"
 #include "ptx.cuh"
@@ -107,11 +109,19 @@ __global__ void k_stencil_generic(const T* __restrict__ psi, const T* __restrict
 }
 
 // ---- TMA plane-marching kernel ---------------------------------------------------
-constexpr int kBZ = 32;       // tile width along z (one warp)
+constexpr int kBZ = 32;       // tile width along z
 constexpr int kBY = 32;       // tile height along y
-constexpr int kTY = 8;        // thread rows; each thread owns kYPT consecutive y rows
-constexpr int kYPT = kBY / kTY;
+constexpr int kZP = kBZ / 2;  // threads along z: each owns two consecutive z points
 constexpr int kSlots = 6;     // plane ring depth: 3 planes of look-ahead, 3 FP32 (2 FP64) CTAs per SM
+
+template <typename T> struct Pair;
+template <> struct Pair<float> { using type = float2; };
+template <> struct Pair<double> { using type = double2; };
+
+template <typename T>
+__device__ __forceinline__ typename Pair<T>::type ld2(const T* p) {
+  return *reinterpret_cast<const typename Pair<T>::type*>(p);
+}
 
 template <typename T, int R>
 struct TmaGeom {
@@ -125,29 +135,40 @@ struct TmaGeom {
   static constexpr int SMEM = kSlots * SLOT_BYTES + kSlots * 8 + 128;
 };
 
+// Runs step(slot 0), step(slot 1), ... in order until one returns false.
+template <typename F, int... Js>
+__device__ __forceinline__ bool run_slots(F& step, int qb, std::integer_sequence<int, Js...>) {
+  return (step(std::integral_constant<int, Js>{}, qb) && ...);
+}
+
 // One CTA: a kBY x kBZ column of one field, planes [xs, xs + cx) along x.
 // Plane q of the chunk is x = xs - R + q and sits in ring slot q % kSlots; it
 // feeds the x register queue at iteration q and is the centre plane at
 // iteration q + R, after which its slot is refilled with plane q + kSlots.
 // The plane loop is unrolled by the ring depth, so slot addresses are
-// immediates and the queue shifts are register renames. Each thread owns
-// rows yt .. yt + kYPT - 1 at z = tz: its y neighbours are its own queue
-// centres plus 2R halo rows, its z neighbours are shared-memory reads.
-template <typename T, int R, bool HAS_V, bool STORE, bool DOT>
-__global__ void __launch_bounds__(kBZ* kTY)
+// immediates and the queue shifts are register renames. Each thread owns the
+// z pair (z, z + 1) of YPT consecutive rows: every shared-memory access moves
+// a pair (8 bytes FP32, 16 bytes FP64), the z neighbours of both points come
+// from two pair loads (z - 2, z - 1) and (z + 2, z + 3), the y neighbours are
+// the thread's own queue centres plus 2R halo rows, and the output leaves as
+// one pair store per row.
+template <typename T, int R, int YPT, bool HAS_V, bool STORE, bool DOT>
+__global__ void __launch_bounds__(kZP*(kBY / YPT))
     k_stencil_tma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap vmap,
                   T* __restrict__ out, int nx, int ny, int nz, int cx, int tiles_z, int64_t bstride,
                   T coef, double* dot_part, int* err) {
   using G = TmaGeom<T, R>;
+  using P2 = typename Pair<T>::type;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  unsigned char* smem =
-      (unsigned char*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
+  // 128-byte aligned ring; offsetting the shared array itself keeps every
+  // ring access a shared-memory access
+  unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kSlots * G::SLOT_BYTES);
   __shared__ double sh[32];
 
   const StencilCoef<T> c = coefs<T>(R == 1 ? 2 : 4);
   const int tz = threadIdx.x, ty = threadIdx.y;
-  const int tid = ty * kBZ + tz;
+  const int tid = ty * kZP + tz;
   const int tile_z = blockIdx.x % tiles_z, tile_y = blockIdx.x / tiles_z;
   const int z0 = tile_z * kBZ, y0 = tile_y * kBY;
   const int xs = blockIdx.y * cx;
@@ -175,79 +196,98 @@ __global__ void __launch_bounds__(kBZ* kTY)
     for (int q = 0; q < issued; ++q) issue(q);
   }
 
-  const int yt = ty * kYPT;
-  const int gz = z0 + tz;
+  const int yt = ty * YPT;
+  const int gz = z0 + 2 * tz;   // nz is even, so a pair is wholly inside or outside
   unsigned live = 0;
 #pragma unroll
-  for (int k = 0; k < kYPT; ++k)
+  for (int k = 0; k < YPT; ++k)
     if (gz < nz && y0 + yt + k < ny) live |= 1u << k;
   T* obase = nullptr;
   if (STORE) obase = out + (int64_t)b * bstride + ((int64_t)xs * ny + (y0 + yt)) * nz + gz;
   const int64_t pstride = (int64_t)ny * nz;
-  const int cidx = (yt + R) * G::PW + tz + G::A;   // this thread's first row, centre column
+  const int cidx = (yt + R) * G::PW + 2 * tz + G::A;   // first row, centre pair (even index)
+  const int vidx = yt * kBZ + 2 * tz;
 
-  T xq[kYPT][2 * R + 1];
+  P2 xq[YPT][2 * R + 1];
 #pragma unroll
-  for (int k = 0; k < kYPT; ++k)
+  for (int k = 0; k < YPT; ++k)
 #pragma unroll
-    for (int r = 0; r < 2 * R + 1; ++r) xq[k][r] = (T)0;
+    for (int r = 0; r < 2 * R + 1; ++r) xq[k][r].x = xq[k][r].y = (T)0;
   Acc<T> acc;
   bool bad = false;
   int q = 0;
-  for (int qb = 0; qb < P && !bad; qb += kSlots) {
+  T* op = obase;   // output row of the next centre plane
+  // One plane step with ring slot J a compile-time constant, so slot addresses
+  // are immediates and the x-queue shifts are register renames; false ends
+  // the march (end of the chunk, or a timed-out wait anywhere in the CTA).
+  auto step = [&](auto slot, int qb) -> bool {
+    constexpr int J = decltype(slot)::value;
+    q = qb + J;
+    if (q >= P) return false;
+    if (!mbar_wait_bounded(&bars[J], (uint32_t)((qb / kSlots) & 1), err, 101)) bad = true;
+    const T* pl = reinterpret_cast<const T*>(smem + J * G::SLOT_BYTES);
 #pragma unroll
-    for (int j = 0; j < kSlots; ++j) {
-      q = qb + j;
-      if (q >= P) break;
-      if (!mbar_wait_bounded(&bars[j], (uint32_t)((qb / kSlots) & 1), err, 101)) bad = true;
-      const T* pl = reinterpret_cast<const T*>(smem + j * G::SLOT_BYTES);
+    for (int k = 0; k < YPT; ++k) {
 #pragma unroll
-      for (int k = 0; k < kYPT; ++k) {
+      for (int r = 0; r < 2 * R; ++r) xq[k][r] = xq[k][r + 1];
+      xq[k][2 * R] = ld2(pl + cidx + k * G::PW);
+    }
+    if (q >= 2 * R) {
+      constexpr int CS = (J + kSlots - R) % kSlots;
+      const T* pc = reinterpret_cast<const T*>(smem + CS * G::SLOT_BYTES);
+      [[maybe_unused]] const T* pv = reinterpret_cast<const T*>(smem + CS * G::SLOT_BYTES + G::V_OFF);
+      P2 col[YPT + 2 * R];
 #pragma unroll
-        for (int r = 0; r < 2 * R; ++r) xq[k][r] = xq[k][r + 1];
-        xq[k][2 * R] = pl[cidx + k * G::PW];
+      for (int i = 0; i < R; ++i) {
+        col[i] = ld2(pc + cidx + (i - R) * G::PW);
+        col[R + YPT + i] = ld2(pc + cidx + (YPT + i) * G::PW);
       }
-      if (q >= 2 * R) {
-        const int cs = (j + kSlots - R) % kSlots;   // compile-time after unrolling
-        const T* pc = reinterpret_cast<const T*>(smem + cs * G::SLOT_BYTES);
-        const T* pv = reinterpret_cast<const T*>(smem + cs * G::SLOT_BYTES + G::V_OFF);
-        T col[kYPT + 2 * R];
 #pragma unroll
-        for (int i = 0; i < R; ++i) {
-          col[i] = pc[cidx + (i - R) * G::PW];
-          col[R + kYPT + i] = pc[cidx + (kYPT + i) * G::PW];
+      for (int k = 0; k < YPT; ++k) col[R + k] = xq[k][R];
+#pragma unroll
+      for (int k = 0; k < YPT; ++k) {
+        const int idx = cidx + k * G::PW;
+        const P2 ctr = xq[k][R];
+        const P2 lo = ld2(pc + idx - 2), hi = ld2(pc + idx + 2);   // (z-2, z-1), (z+2, z+3)
+        // point z in .x, point z + 1 in .y; neighbour order x, y, z as in the reference sum
+        T s1a = xq[k][R - 1].x + xq[k][R + 1].x + col[R + k - 1].x + col[R + k + 1].x + lo.y + ctr.y;
+        T s1b = xq[k][R - 1].y + xq[k][R + 1].y + col[R + k - 1].y + col[R + k + 1].y + ctr.x + hi.x;
+        T s2a = (T)0, s2b = (T)0;
+        if constexpr (R == 2) {
+          s2a = xq[k][0].x + xq[k][4].x + col[k].x + col[k + 4].x + lo.x + hi.x;
+          s2b = xq[k][0].y + xq[k][4].y + col[k].y + col[k + 4].y + lo.y + hi.y;
         }
-#pragma unroll
-        for (int k = 0; k < kYPT; ++k) col[R + k] = xq[k][R];
-        T* op = STORE ? obase + (int64_t)(q - 2 * R) * pstride : nullptr;
-#pragma unroll
-        for (int k = 0; k < kYPT; ++k) {
-          const int idx = cidx + k * G::PW;
-          const T ctr = xq[k][R];
-          T s1 = xq[k][R - 1] + xq[k][R + 1] + col[R + k - 1] + col[R + k + 1] + pc[idx - 1] +
-                 pc[idx + 1];
-          T s2 = (T)0;
-          if constexpr (R == 2)
-            s2 = xq[k][0] + xq[k][4] + col[k] + col[k + 4] + pc[idx - 2] + pc[idx + 2];
-          T val = coef * lap_combine<T>(ctr, s1, s2, c, R);
-          if constexpr (HAS_V) val += pv[(yt + k) * kBZ + tz] * ctr;
-          if (live & (1u << k)) {
-            if constexpr (STORE) op[k * nz] = val;
-            if constexpr (DOT) acc.add_prod(ctr, val);
+        P2 val;
+        val.x = coef * lap_combine<T>(ctr.x, s1a, s2a, c, R);
+        val.y = coef * lap_combine<T>(ctr.y, s1b, s2b, c, R);
+        if constexpr (HAS_V) {
+          const P2 v = ld2(pv + vidx + k * kBZ);
+          val.x += v.x * ctr.x;
+          val.y += v.y * ctr.y;
+        }
+        if (live & (1u << k)) {
+          if constexpr (STORE) *reinterpret_cast<P2*>(op + k * nz) = val;
+          if constexpr (DOT) {
+            acc.add_prod(ctr.x, val.x);
+            acc.add_prod(ctr.y, val.y);
           }
         }
       }
-      // every thread is done with plane q - R; a timed-out wait anywhere stops the CTA
-      if (__syncthreads_or(bad)) {
-        bad = true;
-        break;
-      }
-      if (tid == 0 && q >= R && q - R + kSlots < P) {
-        issue(q - R + kSlots);
-        ++issued;
-      }
+      if constexpr (STORE) op += pstride;
     }
-  }
+    // every thread is done with plane q - R; a timed-out wait anywhere stops the CTA
+    if (__syncthreads_or(bad)) {
+      bad = true;
+      return false;
+    }
+    if (tid == 0 && q >= R && q - R + kSlots < P) {
+      issue(q - R + kSlots);
+      ++issued;
+    }
+    return true;
+  };
+  for (int qb = 0; qb < P; qb += kSlots)
+    if (!run_slots(step, qb, std::make_integer_sequence<int, kSlots>{})) break;
   if (bad) {
     // drain the copies still in flight (bounded) before the CTA's shared memory goes away
     if (tid == 0)
@@ -263,24 +303,30 @@ __global__ void __launch_bounds__(kBZ* kTY)
   }
 }
 
+// Rows per thread of the TMA kernel: 4 (128-thread CTAs) or 2 (256-thread
+// CTAs); 0 picks the default. Process-wide, set by the autotuner.
+std::atomic<int> g_rows_per_thread{0};
+constexpr int kDefaultRows = 2;
+
 // Resident CTAs of a kernel on the whole GPU (occupancy x SMs).
 template <typename K>
-int resident_ctas(K kernel, int smem) {
+int resident_ctas(K kernel, int threads, int smem) {
   int dev = 0, sms = 0, per = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kBZ * kTY, smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem) != cudaSuccess ||
       per <= 0)
     return 152;
   return per * sms;
 }
 
-template <typename T, int R, bool HAS_V, bool STORE, bool DOT>
-int launch_tma_mode(const CUtensorMap& tm, const CUtensorMap& vm, void* out, int nb, int nx, int ny,
+template <typename T, int R, int YPT, bool HAS_V, bool STORE, bool DOT>
+int launch_tma_rows(const CUtensorMap& tm, const CUtensorMap& vm, void* out, int nb, int nx, int ny,
                     int nz, int64_t bstride, double coef, double* dot_part, int* nparts,
                     cudaStream_t s) {
   using G = TmaGeom<T, R>;
-  auto kern = k_stencil_tma<T, R, HAS_V, STORE, DOT>;
+  constexpr int kThreads = kZP * (kBY / YPT);
+  auto kern = k_stencil_tma<T, R, YPT, HAS_V, STORE, DOT>;
   // opt in to the large shared-memory carve-out once per device (the launch
   // itself then issues only stream work, so it can be graph-captured)
   static std::atomic<unsigned> attr_done{0};
@@ -296,12 +342,12 @@ int launch_tma_mode(const CUtensorMap& tm, const CUtensorMap& vm, void* out, int
   // Split x into chunks so the grid is one full resident wave where the
   // problem allows (every CTA streams at once, no tail wave); a chunk keeps at
   // least 4 planes, since its 2R halo planes are re-read.
-  static const int cap = resident_ctas(kern, G::SMEM);   // one value per instantiation
+  static const int cap = resident_ctas(kern, kThreads, G::SMEM);   // one value per instantiation
   int chunks = (int)std::max<int64_t>(1, cap / ((int64_t)tiles * nb));
   chunks = std::min(chunks, std::max(1, nx / 4));
   const int cx = (nx + chunks - 1) / chunks;
   chunks = (nx + cx - 1) / cx;
-  dim3 grid(tiles, chunks, nb), block(kBZ, kTY);
+  dim3 grid(tiles, chunks, nb), block(kZP, kBY / YPT);
   if (nparts) *nparts = tiles * chunks;
   kern<<<grid, block, G::SMEM, s>>>(tm, vm, (T*)out, nx, ny, nz, cx, tiles_z, bstride, (T)coef,
                                     dot_part, device_error_word());
@@ -309,6 +355,17 @@ int launch_tma_mode(const CUtensorMap& tm, const CUtensorMap& vm, void* out, int
   return GATO_OK;
 }
 
+template <typename T, int R, bool HAS_V, bool STORE, bool DOT>
+int launch_tma_mode(const CUtensorMap& tm, const CUtensorMap& vm, void* out, int nb, int nx, int ny,
+                    int nz, int64_t bstride, double coef, double* dot_part, int* nparts,
+                    cudaStream_t s) {
+  const int rows = g_rows_per_thread.load() ? g_rows_per_thread.load() : kDefaultRows;
+  if (rows == 2)
+    return launch_tma_rows<T, R, 2, HAS_V, STORE, DOT>(tm, vm, out, nb, nx, ny, nz, bstride, coef,
+                                                       dot_part, nparts, s);
+  return launch_tma_rows<T, R, 4, HAS_V, STORE, DOT>(tm, vm, out, nb, nx, ny, nz, bstride, coef,
+                                                     dot_part, nparts, s);
+}
 template <typename T, int R>
 int launch_tma(const void* psi, const void* V, void* out, int nb, int nx, int ny, int nz,
                int64_t bstride, double coef, double* dot_part, int* nparts, cudaStream_t s) {
@@ -369,7 +426,8 @@ int stencil_typed(const void* psi, const void* V, void* out, int nb, int nx, int
                   double dv, cudaStream_t s) {
   const bool tma_ok = boundary == GATO_DIRICHLET && ((uint64_t)nz * sizeof(T)) % 16 == 0 &&
                       ((uint64_t)bstride * sizeof(T)) % 16 == 0 &&
-                      ((uintptr_t)psi % 16) == 0 && ((uintptr_t)V % 16) == 0 && nb <= 65535;
+                      ((uintptr_t)psi % 16) == 0 && ((uintptr_t)V % 16) == 0 &&
+                      ((uintptr_t)out % 16) == 0 && nb <= 65535;
   double* part = nullptr;
   if (dot_dev) {
     // worst case: generic path uses kRedBlocks partials per batch.
@@ -428,7 +486,19 @@ int stencil_apply(int dtype, const void* psi, const void* V, void* out, int nb, 
   return fail(GATO_EBADARG, "bad dtype %d", dtype);
 }
 
+int stencil_tune(int rows_per_thread) {
+  if (rows_per_thread != 0 && rows_per_thread != 2 && rows_per_thread != 4)
+    return fail(GATO_EBADARG, "stencil tune: rows per thread must be 0, 2 or 4, got %d",
+                rows_per_thread);
+  g_rows_per_thread.store(rows_per_thread);
+  return GATO_OK;
+}
+
 }  // namespace gato
+
+extern "C" int gato_stencil_tune(int rows_per_thread) {
+  return gato::stencil_tune(rows_per_thread);
+}
 
 extern "C" int gato_stencil_apply(int dtype, const void* psi, const void* V, void* out, int nb,
                                   int nx, int ny, int nz, double lap_coef, int boundary,

@@ -89,6 +89,10 @@ int gato_normalize(int dtype, void* a, int64_t n, const double* norm_sq_dev, voi
 int gato_stencil_apply(int dtype, const void* psi, const void* V, void* out, int nb,
                        int nx, int ny, int nz, double lap_coef, int boundary, int order,
                        double* dot_dev, double dv, void* stream);
+/* Tile shape of the stencil's TMA kernel: rows per thread 4 (128-thread
+ * CTAs) or 2 (256-thread CTAs), 0 = default. Process-wide; chosen by the
+ * autotuner. No reference counterpart (a tuning knob of this library).   */
+int gato_stencil_tune(int rows_per_thread);
 
 /* ---- potentials.py / pseudopotentials.py --------------------------------
  * V = -sum_k Z_k / sqrt(|r-R_k|^2 + eps^2): potentials.py:16-61.

@@ -67,6 +67,35 @@ def test_laplacian_shapes(shape, order):
         assert rel_err(host(laplacian(dev(psi), 0.3, b, order)), o.laplacian(psi, 0.3, b, order)) < 1e-11
 
 
+@pytest.mark.parametrize("rows", [2, 4])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("order", [2, 4])
+def test_stencil_tile_variants(rows, dtype, order):
+    """Both TMA tile shapes (rows per thread) against the oracle: Hamiltonian
+    apply with V, the fused <psi, H psi>, a block of fields, partial tiles in
+    y and z and chunked x."""
+    from gato_gb300 import _lib
+    from gato_gb300.operators import stencil
+    rng = np.random.default_rng(7 + rows)
+    shape = (3, 40, 36, 44)                 # 44 z: one full and one partial 32-wide tile
+    psi = rng.standard_normal(shape)
+    V = rng.standard_normal(shape[1:])
+    if dtype == torch.float32:
+        psi, V = psi.astype(np.float32).astype(np.float64), V.astype(np.float32).astype(np.float64)
+    h, coef = 0.3, -0.5 / 0.09
+    _lib.call("gato_stencil_tune", rows)
+    try:
+        out, dots = stencil(dev(psi, dtype), h, "dirichlet", order, coef, V=dev(V, dtype), dot=True)
+    finally:
+        _lib.call("gato_stencil_tune", 0)
+    ref = np.stack([coef * o.laplacian(p, h, "dirichlet", order) / (1.0 / h ** 2) + V * p for p in psi])
+    assert rel_err(host(out), ref) < FTOL[dtype]
+    ref_dots = [float(np.sum(p * r)) * h ** 3 for p, r in zip(psi, ref)]
+    tol = 1e-11 if dtype == torch.float64 else 1e-6
+    for got, want in zip(host(dots), ref_dots):
+        assert abs(got - want) < tol * max(abs(want), 1.0)
+
+
 def test_complex_plane_wave_kat():                      # reference test_laplacian.py:24-38
     from gato_gb300.operators import laplacian
     N, L = 32, 4.0
