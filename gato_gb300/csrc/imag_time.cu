@@ -30,10 +30,10 @@ __global__ void k_scale_rsqrt(const T* src, T* dst, int64_t n, const double* nsq
   __shared__ double sc;   // one FP64 reciprocal square root per block
   if (threadIdx.x == 0) sc = 1.0 / sqrt(nsq[0]);
   __syncthreads();
-  const double s = sc;
+  const T s = (T)sc;   // products in the field type (FP64 per element is slow on GB300)
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
-    dst[i] = (T)((double)src[i] * s);
+    dst[i] = src[i] * s;
 }
 
 __global__ void k_div_store(const double* num, const double* den, double* out) {

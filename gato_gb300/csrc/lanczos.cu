@@ -450,7 +450,10 @@ __global__ void __launch_bounds__(kBulkThreads)
 
 // beta = sqrt(nrm); v = W / beta (or 0); betas_out[0] = beta
 // (the square root and the reciprocal are FP64 and cost many FP64-pipe
-// instructions on GB300, so one thread per block computes them)
+// instructions on GB300, so one thread per block computes them; the
+// per-element products run in the field type: an FP32 basis takes the FP64
+// reciprocal rounded once to FP32, as FP64 products would put three FP64-pipe
+// operations on every element)
 template <typename T>
 __global__ void k_beta_scale(T* W, int64_t n, const double* nrm, double* beta_out) {
   __shared__ double sb[2];
@@ -461,10 +464,11 @@ __global__ void k_beta_scale(T* W, int64_t n, const double* nrm, double* beta_ou
     if (blockIdx.x == 0) beta_out[0] = beta;
   }
   __syncthreads();
-  const double beta = sb[0], inv = sb[1];
+  const bool pos = sb[0] > 0;
+  const T inv = (T)sb[1];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
-    W[i] = beta > 0 ? (T)((double)W[i] * inv) : (T)0;
+    W[i] = pos ? W[i] * inv : (T)0;
 }
 
 template <typename T>
@@ -472,10 +476,10 @@ __global__ void k_scale_copy(const T* __restrict__ src, T* dst, int64_t n, const
   __shared__ double sc;   // one FP64 reciprocal square root per block
   if (threadIdx.x == 0) sc = 1.0 / sqrt(nrm[0]);
   __syncthreads();
-  const double inv = sc;
+  const T inv = (T)sc;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
-    dst[i] = (T)((double)src[i] * inv);
+    dst[i] = src[i] * inv;
 }
 
 

@@ -174,6 +174,12 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   }
 }
 
+// Padded length of a staged input row: N rounded up to RMAX modulo 32 words.
+template <int R1, int R2> struct StageRow {
+  static constexpr int N = R1 * R2 / 2, RM = Shape<R1, R2>::RMAX;
+  static constexpr int NP = N + ((RM - N % 32) % 32 + 32) % 32;
+};
+
 // The inputs a launch group of pair fields reads, staged once per CTA by
 // k_rows_fwd_multi: slot_of[i] is input i's staging slot (-1: unused).
 struct RowsIn {
@@ -186,13 +192,15 @@ struct RowsIn {
 // input (the orbitals, psi) are staged in shared memory once, then each field's
 // pair densities are formed straight into the stage-1 registers of its FFT.
 // Same transform and output as k_rows_fwd, without re-reading the inputs per
-// field. Staged rows are padded to N + 1; stage-1 lanes read consecutive z.
+// field. Stage-1 lanes read consecutive z of RMAX-lane lines, so a staged row
+// is padded to a multiple of 32 words plus RMAX (StageRow): the lines a warp
+// reads fall in disjoint bank ranges.
 template <typename T, int R1, int R2, int L>
 __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
     k_rows_fwd_multi(PassArgs args, RowsIn ri, int f0, int nfg, typename Cplx<T>::type* S1,
                      const typename Cplx<T>::type* tw) {
   using T2 = typename Cplx<T>::type;
-  constexpr int M = R1 * R2, N = M / 2, NP = N + 1, RM = Shape<R1, R2>::RMAX, NT = L * RM;
+  constexpr int M = R1 * R2, N = M / 2, NP = StageRow<R1, R2>::NP, RM = Shape<R1, R2>::RMAX, NT = L * RM;
   extern __shared__ __align__(16) unsigned char smraw[];
   T2* buf = reinterpret_cast<T2*>(smraw);
   T2* tws = buf + L * RowBuf<R1, R2>::LS;
@@ -473,12 +481,16 @@ struct Launch {
         use(d.a);
         use(d.b);
       }
-    const size_t stage_bytes = (size_t)ri.nin * L * (N + 1) * sizeof(T);
+    // half the rows per CTA of the other z kernels: the grid covers every
+    // field at once, so smaller CTAs give more of them and a shorter last wave
+    constexpr int LM = L >= 16 ? L / 2 : L;
+    const size_t stage_bytes = (size_t)ri.nin * LM * StageRow<R1, R2>::NP * sizeof(T);
     if (nfg >= 3 && stage_bytes <= 48 * 1024) {
-      const size_t sm = sm_rows() + stage_bytes;
-      GATO_TRY(smem_attr(k_rows_fwd_multi<T, R1, R2, L>, sm));
+      const size_t sm = (size_t)(LM * RowBuf<R1, R2>::LS + TWN) * sizeof(T2) + stage_bytes;
+      GATO_TRY(smem_attr(k_rows_fwd_multi<T, R1, R2, LM>, sm));
       const int64_t nrows = (int64_t)N * N;
-      k_rows_fwd_multi<T, R1, R2, L><<<(unsigned)((nrows + L - 1) / L), NT, sm, s>>>(a, ri, f0, nfg, S1, tw);
+      k_rows_fwd_multi<T, R1, R2, LM><<<(unsigned)((nrows + LM - 1) / LM), LM * Shape<R1, R2>::RMAX, sm, s>>>(
+          a, ri, f0, nfg, S1, tw);
       GATO_LAUNCH_TRY();
       return GATO_OK;
     }
