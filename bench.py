@@ -192,6 +192,7 @@ def e2e_pipelined(st, g, host_in, steps):
     op2 = Operator(g, torch.float32, 4, "dirichlet")
     op2.set_potential(st["op"]._keep["V"])
     op2.set_nonlocal(st["op"]._keep["nl"])
+    op2.tune(st["op"].block_epilogue)
     bufs.append(torch.empty_like(st["fields"]))
     op2.set_exchange(st["plan"], bufs[1])
     ops.append(op2)
@@ -329,10 +330,15 @@ def run_gato(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     from gato_gb300.autotune import tune_plan
     tuned = {}
+    from gato_gb300.autotune import tune_block_epilogue
     for name, st in (("mixed", s32), ("fp64", s64)):
-        best = tune_plan(st["plan"], lambda st=st: st["op"].apply_block(st["out"]), key="block")
+        step = lambda st=st: st["op"].apply_block(st["out"])  # noqa: E731
+        best = tune_plan(st["plan"], step, key="block")
+        epi = tune_block_epilogue(st["op"], step, key="block")
         tuned[name] = {"group": best["group"], "engine": best["engine"],
-                       "candidates_ms": {str(c["group"]): round(c["ms"], 4) for c in best["candidates"]}}
+                       "candidates_ms": {str(c["group"]): round(c["ms"], 4) for c in best["candidates"]},
+                       "block_epilogue": epi["epilogue"],
+                       "epilogue_ms": {str(c["epilogue"]): round(c["ms"], 4) for c in epi["candidates"]}}
 
     def timed(fn, steps, warmup):
         for _ in range(warmup):

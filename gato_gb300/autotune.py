@@ -86,3 +86,22 @@ def tune_stencil(step, key=None, reps: int = 5) -> dict:
     _lib.call("gato_stencil_tune", best["rows"])
     _CACHE[key] = best
     return best
+
+
+def tune_block_epilogue(op, step, key=None, reps: int = 5) -> dict:
+    """Pick the block-apply epilogue of operator `op` that runs `step()` fastest:
+    1 = the J_ij fields and one pair pass, 2 = accumulation in the z-inverse epilogue."""
+    key = ("block_epi", op.grid.N, op.dtype, key)
+    if key in _CACHE:
+        best = _CACHE[key]
+        op.tune(best["epilogue"])
+        return best
+    results = []
+    for epi in (1, 2):
+        op.tune(epi)
+        results.append({"epilogue": epi, "ms": _time(step, reps)})
+    best = min(results, key=lambda r: r["ms"])
+    best = dict(best, candidates=results)
+    op.tune(best["epilogue"])
+    _CACHE[key] = best
+    return best

@@ -448,26 +448,43 @@ __global__ void __launch_bounds__(kBulkThreads)
   if (threadIdx.x == 0 && !*abort_v) part[blockIdx.x] = sum;
 }
 
-// beta = sqrt(nrm); v = W / beta (or 0); betas_out[0] = beta
-// (the square root and the reciprocal are FP64 and cost many FP64-pipe
-// instructions on GB300, so one thread per block computes them; the
-// per-element products run in the field type: an FP32 basis takes the FP64
-// reciprocal rounded once to FP32, as FP64 products would put three FP64-pipe
-// operations on every element)
-template <typename T>
-__global__ void k_beta_scale(T* W, int64_t n, const double* nrm, double* beta_out) {
-  __shared__ double sb[2];
+// nrm = dV * sum of the norm partials (the k_finalize_sums reduction order),
+// beta = sqrt(nrm) -> binv[0] and betas_out[0], 1 / beta (0 if beta = 0) ->
+// binv[1]: the FP64 square root and reciprocal once per step, in one thread.
+__global__ void k_beta_finalize(const double* partials, int nparts, double scale, double* binv,
+                                double* beta_out) {
+  __shared__ double sh[32];
+  double v = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) v += partials[i];
+  v = block_sum(v, sh);
   if (threadIdx.x == 0) {
-    const double beta = sqrt(nrm[0]);
-    sb[0] = beta;
-    sb[1] = beta > 0 ? 1.0 / beta : 0.0;
-    if (blockIdx.x == 0) beta_out[0] = beta;
+    const double beta = sqrt(v * scale);
+    binv[0] = beta;
+    binv[1] = beta > 0 ? 1.0 / beta : 0.0;
+    beta_out[0] = beta;
   }
-  __syncthreads();
-  const bool pos = sb[0] > 0;
-  const T inv = (T)sb[1];
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
+}
+
+// v = W / beta (or 0). The products run in the field type: an FP32 basis takes
+// the FP64 reciprocal rounded once to FP32, as FP64 products would put three
+// FP64-pipe operations on every element on GB300.
+template <typename T>
+__global__ void k_beta_scale(T* W, int64_t n, const double* binv) {
+  using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  constexpr int VEC = 16 / (int)sizeof(T);
+  const bool pos = binv[0] > 0;
+  const T inv = (T)binv[1];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nv = ((uintptr_t)W % 16) == 0 ? n / VEC : 0;   // 16-byte vectors
+  V* W4 = reinterpret_cast<V*>(W);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride) {
+    V v = W4[i];
+    T* e = reinterpret_cast<T*>(&v);
+#pragma unroll
+    for (int u = 0; u < VEC; ++u) e[u] = pos ? e[u] * inv : (T)0;
+    W4[i] = v;
+  }
+  for (int64_t i = nv * VEC + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
     W[i] = pos ? W[i] * inv : (T)0;
 }
 
@@ -483,186 +500,246 @@ __global__ void k_scale_copy(const T* __restrict__ src, T* dst, int64_t n, const
 }
 
 
-// ---- tridiagonal eigensolver (FP64, one block) ----------------------------------
+// ---- tridiagonal eigensolver (FP64) ----------------------------------------------
 
-// number of eigenvalues of T strictly below x (Sturm count via LDL^T pivots)
-__device__ int sturm_count(const double* a, const double* e2, int m, double x, double pivmin) {
-  int cnt = 0;
-  double q = a[0] - x;
-  if (fabs(q) < pivmin) q = -pivmin;
-  if (q < 0) ++cnt;
+// Number of eigenvalues of T below x: the sign changes of the leading principal
+// minors p_i = det(T_i - x I), p_0 = 1, p_1 = a_0 - x,
+// p_{i+1} = (a_i - x) p_i - e_{i-1}^2 p_{i-1} (the Sturm sequence of Wilkinson,
+// The Algebraic Eigenvalue Problem, ch. 5). No division: three FP64 operations
+// a step instead of a division chain, which GB300's narrow FP64 pipe makes
+// long. A zero minor takes the sign opposite to its predecessor (the LDL^T
+// form's q_i = 0 -> -pivmin convention), and the pair (p_i, p_{i-1}) is
+// rescaled by an exact power of two whenever p_i's exponent leaves [-480, 480].
+__device__ int sturm_count(const double* a, const double* e2, int m, double x) {
+  auto neg = [](double v, bool prev_neg) {
+    const int hi = __double2hiint(v);
+    const bool zero = ((hi & 0x7fffffff) | __double2loint(v)) == 0;
+    return zero ? !prev_neg : hi < 0;
+  };
+  double pm = 1.0, p = a[0] - x;
+  bool s = neg(p, false);
+  int cnt = s;
   for (int i = 1; i < m; ++i) {
-    q = (a[i] - x) - e2[i - 1] / q;
-    if (fabs(q) < pivmin) q = -pivmin;
-    if (q < 0) ++cnt;
+    const double pn = fma(a[i] - x, p, -e2[i - 1] * pm);
+    const bool sn = neg(pn, s);
+    cnt += sn != s;
+    pm = p;
+    p = pn;
+    s = sn;
+    const int ex = (__double2hiint(p) >> 20) & 0x7ff;
+    if (ex > 1023 + 480) {
+      p *= 0x1p-480;
+      pm *= 0x1p-480;
+    } else if (ex < 1023 - 480 && p != 0.0) {
+      p *= 0x1p480;
+      pm *= 0x1p480;
+    }
   }
   return cnt;
 }
 
-// Shared: a[m], e[m], e2[m]; eigenvalues -> lam[K]; eigenvectors -> Y[m*K] (column k at Y + k*m)
-// work: global scratch of 5*m*K doubles for the LU factors.
-__global__ void __launch_bounds__(256) k_tridiag_eig(const double* alpha, const double* beta, int m, int K, double* evals,
-                              double* Y, double* work, int* flag, double tol, int* err) {
+// Gershgorin bound of T = diag(a) + offdiag(e): lower and upper ends and the
+// norm max_i |a_i| + r_i (min/max are exact, so any reduction order agrees).
+__device__ __forceinline__ void gershgorin(const double* a, const double* e, int m, double& lo, double& hi,
+                                           double& nm) {
+  lo = 1e300;
+  hi = -1e300;
+  nm = 0;
+  for (int i = threadIdx.x; i < m; i += 32) {
+    const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < m - 1 ? fabs(e[i]) : 0.0);
+    lo = fmin(lo, a[i] - r);
+    hi = fmax(hi, a[i] + r);
+    nm = fmax(nm, fabs(a[i]) + r);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    nm = fmax(nm, __shfl_xor_sync(0xffffffffu, nm, o));
+  }
+}
+
+// One warp per block, block k = eigenvalue k of T = diag(alpha) +
+// offdiag(beta[:m-1]) (ascending). Multisection on Sturm counts (33
+// sub-intervals a round), then inverse iteration: T - lambda_k I is factored
+// once with partial pivoting (the LAPACK dgttrf scheme: multipliers,
+// interchanges and reciprocal pivots kept in work) and the factors are applied
+// to the iterate four times (dgtts2). One eigenvalue per block spreads the FP64
+// work over K SMs: GB300's FP64 pipe is narrow, and a Sturm count is a chain
+// of m dependent FP64 divisions. work + k*7m: d, du, du2, f, sw, rd, x.
+__global__ void __launch_bounds__(32) k_tridiag_eig(const double* alpha, const double* beta, int m, int K,
+                                                     double* lam_out, double* work, int* err) {
   extern __shared__ double sm[];
   double* a = sm;
   double* e = a + m;
   double* e2 = e + m;
-  double* lam = e2 + m;         // K
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-  for (int i = tid; i < m; i += blockDim.x) {
+  const int lane = threadIdx.x, k = blockIdx.x;
+  for (int i = lane; i < m; i += 32) {
     a[i] = alpha[i];
     e[i] = i < m - 1 ? beta[i] : 0.0;
     e2[i] = e[i] * e[i];
   }
-  __syncthreads();
-  // converged flag: any beta_j < tol for j < max(m-1, 1) (lanczos.py:199)
-  if (tid == 0) {
-    int f = 0;
-    const int lim = m - 1 > 1 ? m - 1 : 1;
-    for (int j = 0; j < lim; ++j) f |= beta[j] < tol;
-    flag[0] = f;
-  }
-  // Gershgorin interval
-  __shared__ double glo, ghi, tnorm;
-  if (tid == 0) {
-    double lo = 1e300, hi = -1e300, nm = 0;
-    for (int i = 0; i < m; ++i) {
-      const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < m - 1 ? fabs(e[i]) : 0.0);
-      lo = fmin(lo, a[i] - r);
-      hi = fmax(hi, a[i] + r);
-      nm = fmax(nm, fabs(a[i]) + r);
-    }
-    const double pad = 2.2e-16 * nm * 4 + 1e-300;
-    glo = lo - pad;
-    ghi = hi + pad;
-    tnorm = nm > 0 ? nm : 1.0;
-  }
-  __syncthreads();
+  __syncwarp();
+  double glo, ghi, nm;
+  gershgorin(a, e, m, glo, ghi, nm);
+  const double pad = 2.2e-16 * nm * 4 + 1e-300;
+  glo -= pad;
+  ghi += pad;
+  const double tnorm = nm > 0 ? nm : 1.0;
   const double pivmin = 1e-290 > 2.2e-16 * 2.2e-16 * tnorm ? 1e-290 : 1e-300;
-  // multisection: warp w finds eigenvalues k = w, w + nw, ...
-  for (int k = warp; k < K; k += nw) {
-    double lo = glo, hi = ghi;
-    for (int it = 0; it < 80; ++it) {
-      const double width = hi - lo;
-      if (width <= 2.2e-16 * 2 * fmax(fabs(lo), fabs(hi)) + pivmin) break;
-      const double x = lo + width * (double)(lane + 1) / 33.0;
-      const int c = sturm_count(a, e2, m, x, pivmin);
-      // bracket: eigenvalue k lies in [x_i, x_{i+1}) where count(x_i) <= k < count(x_{i+1})
-      const unsigned below = __ballot_sync(0xffffffffu, c <= k);   // lanes whose x is <= lambda_k
-      const int nb = __popc(below);  // counts are monotone: lanes 0..nb-1 have c <= k
-      const double nlo = nb > 0 ? lo + width * (double)nb / 33.0 : lo;
-      const double nhi = nb < 32 ? lo + width * (double)(nb + 1) / 33.0 : hi;
-      lo = nlo;
-      hi = nhi;
-    }
-    if (lane == 0) lam[k] = 0.5 * (lo + hi);
+  double lo = glo, hi = ghi;
+  for (int it = 0; it < 80; ++it) {
+    const double width = hi - lo;
+    if (width <= 2.2e-16 * 2 * fmax(fabs(lo), fabs(hi)) + pivmin) break;
+    const double x = lo + width * (double)(lane + 1) / 33.0;
+    const int c = sturm_count(a, e2, m, x);
+    // bracket: eigenvalue k lies in [x_i, x_{i+1}) where count(x_i) <= k < count(x_{i+1})
+    const unsigned below = __ballot_sync(0xffffffffu, c <= k);   // lanes whose x is <= lambda_k
+    const int nb = __popc(below);  // counts are monotone: lanes 0..nb-1 have c <= k
+    const double nlo = nb > 0 ? lo + width * (double)nb / 33.0 : lo;
+    const double nhi = nb < 32 ? lo + width * (double)(nb + 1) / 33.0 : hi;
+    lo = nlo;
+    hi = nhi;
   }
-  __syncthreads();
-  // inverse iteration: thread k computes eigenvector k
-  for (int k = tid; k < K; k += blockDim.x) {
-    double* dl = work + (int64_t)k * 5 * m;
-    double* d = dl + m;
-    double* du = d + m;
-    double* du2 = du + m;
-    double* x = du2 + m;
-    // start vector
-    for (int i = 0; i < m; ++i) x[i] = 1.0 + 0.25 * sin(0.7 * (i + 1) * (k + 1) + 0.3);
-    const double shift = lam[k];
-    const double tiny = 2.2e-16 * tnorm;
-    for (int iter = 0; iter < 4; ++iter) {
-      // factor (T - shift I) with partial pivoting while eliminating the
-      // right-hand side in the same sweep (refactored every iteration: O(m))
-      for (int i = 0; i < m; ++i) {
-        d[i] = a[i] - shift;
-        dl[i] = e[i];
-        du[i] = e[i];
-        du2[i] = 0.0;
+  if (lane != 0) return;
+  const double shift = 0.5 * (lo + hi);
+  lam_out[k] = shift;
+  double* d = work + (int64_t)k * 7 * m;
+  double* du = d + m;
+  double* du2 = du + m;
+  double* f = du2 + m;     // multiplier of step i
+  double* sw = f + m;      // 1.0 where step i interchanged rows i and i+1
+  double* rd = sw + m;     // 1 / d[i] of the final factor
+  double* x = rd + m;
+  const double tiny = 2.2e-16 * tnorm;
+  for (int i = 0; i < m; ++i) {
+    d[i] = a[i] - shift;
+    du[i] = e[i];
+    du2[i] = 0.0;
+  }
+  for (int i = 0; i < m - 1; ++i) {   // factor (dgttrf)
+    const double dli = e[i];
+    if (fabs(d[i]) >= fabs(dli)) {
+      if (d[i] == 0.0) d[i] = tiny;
+      f[i] = dli / d[i];
+      sw[i] = 0.0;
+      d[i + 1] -= f[i] * du[i];
+      du2[i] = 0.0;
+    } else {
+      f[i] = d[i] / dli;
+      sw[i] = 1.0;
+      d[i] = dli;
+      const double t = du[i];
+      du[i] = d[i + 1];
+      d[i + 1] = t - f[i] * d[i + 1];
+      if (i < m - 2) {
+        du2[i] = du[i + 1];
+        du[i + 1] = -f[i] * du[i + 1];
       }
-      // forward elimination applied simultaneously to x (right-hand side)
-      for (int i = 0; i < m - 1; ++i) {
-        if (fabs(d[i]) >= fabs(dl[i])) {
-          if (d[i] == 0.0) d[i] = tiny;
-          const double f = dl[i] / d[i];
-          d[i + 1] -= f * du[i];
-          x[i + 1] -= f * x[i];
-          du2[i] = 0.0;
-        } else {
-          // interchange rows i and i+1
-          const double f = d[i] / dl[i];
-          d[i] = dl[i];
-          const double t = du[i];
-          du[i] = d[i + 1];
-          d[i + 1] = t - f * d[i + 1];
-          if (i < m - 2) {
-            du2[i] = du[i + 1];
-            du[i + 1] = -f * du[i + 1];
-          }
-          const double xt = x[i];
-          x[i] = x[i + 1];
-          x[i + 1] = xt - f * x[i + 1];
-        }
+    }
+  }
+  if (d[m - 1] == 0.0) d[m - 1] = tiny;
+  for (int i = 0; i < m; ++i) rd[i] = 1.0 / d[i];
+  for (int i = 0; i < m; ++i) x[i] = 1.0 + 0.25 * sin(0.7 * (i + 1) * (k + 1) + 0.3);   // start vector
+  for (int iter = 0; iter < 4; ++iter) {
+    for (int i = 0; i < m - 1; ++i) {   // forward: L^-1 P x
+      if (sw[i] == 0.0) {
+        x[i + 1] -= f[i] * x[i];
+      } else {
+        const double xt = x[i];
+        x[i] = x[i + 1];
+        x[i + 1] = xt - f[i] * x[i + 1];
       }
-      if (d[m - 1] == 0.0) d[m - 1] = tiny;
-      // back substitution
-      x[m - 1] /= d[m - 1];
-      if (m > 1) x[m - 2] = (x[m - 2] - du[m - 2] * x[m - 1]) / d[m - 2];
-      for (int i = m - 3; i >= 0; --i) x[i] = (x[i] - du[i] * x[i + 1] - du2[i] * x[i + 2]) / d[i];
-      double nrm = 0.0;
-      for (int i = 0; i < m; ++i) nrm += x[i] * x[i];
+    }
+    x[m - 1] *= rd[m - 1];   // back substitution with U (diagonal, du, du2)
+    if (m > 1) x[m - 2] = (x[m - 2] - du[m - 2] * x[m - 1]) * rd[m - 2];
+    for (int i = m - 3; i >= 0; --i) x[i] = (x[i] - du[i] * x[i + 1] - du2[i] * x[i + 2]) * rd[i];
+    double nrm = 0.0;
+    for (int i = 0; i < m; ++i) nrm += x[i] * x[i];
+    nrm = sqrt(nrm);
+    if (!(nrm > 0) || !isfinite(nrm)) {
+      if (err) atomicExch(err, 201);
+      nrm = 1.0;
+    }
+    const double inv = 1.0 / nrm;
+    for (int i = 0; i < m; ++i) x[i] *= inv;
+  }
+}
+
+// Convergence flag (any beta_j < tol for j < max(m-1, 1), lanczos.py:199),
+// re-orthogonalisation of eigenvectors of clustered eigenvalues, and the sign
+// convention (largest component positive); writes evals and Y (column k at
+// Y + k*m). One thread: O(K^2 m) work at most.
+__global__ void k_tridiag_finish(const double* alpha, const double* beta, int m, int K, const double* lam,
+                                 double* work, double* evals, double* Y, int* flag, double tol) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int fl = 0;
+  const int lim = m - 1 > 1 ? m - 1 : 1;
+  for (int j = 0; j < lim; ++j) fl |= beta[j] < tol;
+  flag[0] = fl;
+  double nm = 0;
+  for (int i = 0; i < m; ++i) {
+    const double r = (i > 0 ? fabs(beta[i - 1]) : 0.0) + (i < m - 1 ? fabs(beta[i]) : 0.0);
+    nm = fmax(nm, fabs(alpha[i]) + r);
+  }
+  const double close = 1e-7 * (nm > 0 ? nm : 1.0);
+  for (int k = 0; k < K; ++k) {
+    double* xk = work + (int64_t)k * 7 * m + 6 * m;
+    for (int l = 0; l < k; ++l) {
+      if (fabs(lam[k] - lam[l]) > close) continue;
+      const double* xl = work + (int64_t)l * 7 * m + 6 * m;
+      double dot = 0;
+      for (int i = 0; i < m; ++i) dot += xl[i] * xk[i];
+      for (int i = 0; i < m; ++i) xk[i] -= dot * xl[i];
+      double nrm = 0;
+      for (int i = 0; i < m; ++i) nrm += xk[i] * xk[i];
       nrm = sqrt(nrm);
-      if (!(nrm > 0) || !isfinite(nrm)) {
-        if (err) atomicExch(err, 201);
-        nrm = 1.0;
-      }
-      for (int i = 0; i < m; ++i) x[i] /= nrm;
+      for (int i = 0; i < m; ++i) xk[i] /= nrm;
     }
-  }
-  __syncthreads();
-  // cluster re-orthogonalisation (thread 0), then sign: largest component positive
-  if (tid == 0) {
-    const double close = 1e-7 * tnorm;
-    for (int k = 0; k < K; ++k) {
-      double* xk = work + (int64_t)k * 5 * m + 4 * m;
-      for (int l = 0; l < k; ++l) {
-        if (fabs(lam[k] - lam[l]) > close) continue;
-        const double* xl = work + (int64_t)l * 5 * m + 4 * m;
-        double dot = 0;
-        for (int i = 0; i < m; ++i) dot += xl[i] * xk[i];
-        for (int i = 0; i < m; ++i) xk[i] -= dot * xl[i];
-        double nrm = 0;
-        for (int i = 0; i < m; ++i) nrm += xk[i] * xk[i];
-        nrm = sqrt(nrm);
-        for (int i = 0; i < m; ++i) xk[i] /= nrm;
-      }
-      int imax = 0;
-      for (int i = 1; i < m; ++i)
-        if (fabs(xk[i]) > fabs(xk[imax])) imax = i;
-      const double sg = xk[imax] < 0 ? -1.0 : 1.0;
-      for (int i = 0; i < m; ++i) Y[(int64_t)k * m + i] = sg * xk[i];
-      evals[k] = lam[k];
-    }
+    int imax = 0;
+    for (int i = 1; i < m; ++i)
+      if (fabs(xk[i]) > fabs(xk[imax])) imax = i;
+    const double sg = xk[imax] < 0 ? -1.0 : 1.0;
+    for (int i = 0; i < m; ++i) Y[(int64_t)k * m + i] = sg * xk[i];
+    evals[k] = lam[k];
   }
 }
 
 // out[k] = sum_j Y[k*m + j] v_j for k in [k0, k0 + KB)
+// The coefficients are rounded to the field type once, in shared memory (a
+// conversion per product would run on GB300's narrow FP64 pipe), and eight
+// basis loads per thread are in flight at a time.
 template <typename T, int KB>
 __global__ void __launch_bounds__(256) k_ritz(const T* __restrict__ V, int64_t ld, int m,
                                               const double* __restrict__ Y, int k0, int K,
                                               T* __restrict__ out, int64_t n) {
-  extern __shared__ double ys[];   // [KB][m]
+  extern __shared__ __align__(16) unsigned char ritz_sm[];
+  T* ys = reinterpret_cast<T*>(ritz_sm);   // [KB][m]
   const int kb = min(KB, K - k0);
-  for (int i = threadIdx.x; i < kb * m; i += blockDim.x) ys[i] = Y[(int64_t)(k0 + i / m) * m + i % m];
+  for (int i = threadIdx.x; i < kb * m; i += blockDim.x) ys[i] = (T)Y[(int64_t)(k0 + i / m) * m + i % m];
   __syncthreads();
+  constexpr int U = 8;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     T acc[KB];
 #pragma unroll
     for (int k = 0; k < KB; ++k) acc[k] = (T)0;
-    for (int j = 0; j < m; ++j) {
+    int j = 0;
+    for (; j + U <= m; j += U) {
+      T v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) v[u] = V[(int64_t)(j + u) * ld + i];
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int k = 0; k < KB; ++k)
+          if (k < kb) acc[k] = fma(ys[k * m + j + u], v[u], acc[k]);
+    }
+    for (; j < m; ++j) {
       const T v = V[(int64_t)j * ld + i];
 #pragma unroll
       for (int k = 0; k < KB; ++k)
-        if (k < kb) acc[k] = fma((T)ys[k * m + j], v, acc[k]);
+        if (k < kb) acc[k] = fma(ys[k * m + j], v, acc[k]);
     }
 #pragma unroll
     for (int k = 0; k < KB; ++k)
@@ -695,8 +772,8 @@ int lz_scratch(cudaStream_t s, int64_t n, int m, int K, LzScratch& z, bool fp64)
   z.nblk_t = lz_nblk_t(n, fp64);
   z.nblk_b = lz_nblk_b(n, fp64);
   const int np = std::max(std::max(z.nblk, z.nblk_t), z.nblk_b);
-  // partials (m+1)*max(grids), coefficients (m+1), norm, Y (m*K), LU work 5*m*K
-  const size_t need = ((size_t)(m + 1) * np + (m + 1) + 8 + (size_t)m * K + (size_t)5 * m * K) *
+  // partials (m+1)*max(grids), coefficients (m+1), norm, Y (m*K), LU work 7*m*K
+  const size_t need = ((size_t)(m + 1) * np + (m + 1) + 8 + (size_t)m * K + (size_t)7 * m * K) *
                       sizeof(double);
   z.part = (double*)stream_scratch(s, need, kSlotLanczos);
   if (!z.part) return fail(GATO_ENOMEM, "lanczos: scratch allocation failed");
@@ -790,8 +867,9 @@ int lz_step(T* Vb, int64_t n, double dV, int j, int passes, double* alphas, doub
       GATO_TRY(finalize_sums(z.part, nk, z.nblk_b, dV, z.coef, s));
       GATO_TRY(gemv_n_bulk<T>(Vb, n, nk, W, pp, z.coef, n, z.nblk_b, z.part, s));
     }
-    GATO_TRY(finalize_sums(z.part, 1, z.nblk_b, dV, z.nrm, s));
-    k_beta_scale<T><<<grid_for(n, 256), 256, 0, s>>>(W, n, z.nrm, betas + j);
+    k_beta_finalize<<<1, 256, 0, s>>>(z.part, z.nblk_b, dV, z.nrm, betas + j);
+    GATO_LAUNCH_TRY();
+    k_beta_scale<T><<<grid_for(n / (16 / (int64_t)sizeof(T)) + 1, 256), 256, 0, s>>>(W, n, z.nrm);
     GATO_LAUNCH_TRY();
     return GATO_OK;
   }
@@ -815,8 +893,9 @@ int lz_step(T* Vb, int64_t n, double dV, int j, int passes, double* alphas, doub
     k_gemv_n<T, float><<<z.nblk, kLzThreads, smn, s>>>(Vb, n, nk, W, pp, z.coef, n, z.part);
     GATO_LAUNCH_TRY();
   }
-  GATO_TRY(finalize_sums(z.part, 1, z.nblk, dV, z.nrm, s));
-  k_beta_scale<T><<<grid_for(n, 256), 256, 0, s>>>(W, n, z.nrm, betas + j);
+  k_beta_finalize<<<1, 256, 0, s>>>(z.part, z.nblk, dV, z.nrm, betas + j);
+  GATO_LAUNCH_TRY();
+  k_beta_scale<T><<<grid_for(n / (16 / (int64_t)sizeof(T)) + 1, 256), 256, 0, s>>>(W, n, z.nrm);
   GATO_LAUNCH_TRY();
   return GATO_OK;
 }
@@ -825,14 +904,15 @@ template <typename T>
 int lz_finish(const T* Vb, int64_t n, int m, int K, double tol, const double* alphas,
               const double* betas, double* evals, T* evecs, int* flag, const LzScratch& z,
               cudaStream_t s) {
-  const size_t sme = (size_t)(3 * m + K + 8) * sizeof(double);
+  const size_t sme = (size_t)3 * m * sizeof(double);
   if (sme > 48 * 1024)
     GATO_CUDA_TRY(cudaFuncSetAttribute(k_tridiag_eig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sme));
-  k_tridiag_eig<<<1, 256, sme, s>>>(alphas, betas, m, K, evals, z.Y, z.work, flag, tol,
-                                     device_error_word());
+  k_tridiag_eig<<<K, 32, sme, s>>>(alphas, betas, m, K, evals, z.work, device_error_word());
+  GATO_LAUNCH_TRY();
+  k_tridiag_finish<<<1, 32, 0, s>>>(alphas, betas, m, K, evals, z.work, evals, z.Y, flag, tol);
   GATO_LAUNCH_TRY();
   constexpr int KB = 4;
-  const size_t smr = (size_t)KB * m * sizeof(double);
+  const size_t smr = (size_t)KB * m * sizeof(T);
   if (smr > 48 * 1024)
     GATO_CUDA_TRY(cudaFuncSetAttribute(k_ritz<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
   for (int k0 = 0; k0 < K; k0 += KB) {

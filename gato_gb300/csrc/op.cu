@@ -5,8 +5,10 @@
 //              subtracts sum_j phi_j J[phi_j psi] in its final z-row epilogue.
 // apply_block: F phi_i for every occupied orbital with the n(n+1)/2 pair
 //              potentials J[phi_i phi_j], each feeding both phi_i and phi_j:
-//              the pipeline writes the J_ij fields, then one elementwise pass
-//              subtracts sum_j phi_j J_ij from every output (each J read once).
+//              either the pipeline writes the J_ij fields and one elementwise
+//              pass subtracts sum_j phi_j J_ij from every output (each J read
+//              once), or the z-inverse epilogue accumulates every output in
+//              registers (no J fields); gato_op_tune picks, the autotuner times both.
 // energy     : kinetic via the stencil's fused <phi, T phi> reduction (no
 //              store), V_ext and V_nl by reductions, E_H and E_x from one
 //              batched pair-solve pass in energy mode (rho with weight 1/2,
@@ -176,7 +178,7 @@ extern "C" int gato_op_apply_block(gato_op_t op, void* out, void* stream) {
   if (op->nl) GATO_TRY(nonlocal_apply(op->nl->n, op->orbitals, out, op->n_orb, s));
   PassArgs a;
   block_pairs(a, *op, out, false);
-  if (poisson_j_supported(op->pp->p)) {
+  if (op->block_epi != 2 && poisson_j_supported(op->pp->p)) {
     // pair potentials to J fields, then one elementwise pass: out_i -= sum_j phi_j J_ij
     const size_t need = (size_t)2 * a.nf * op_n3(*op) * op_esize(*op);
     if (op->jbuf_bytes < need) {
@@ -192,6 +194,13 @@ extern "C" int gato_op_apply_block(gato_op_t op, void* out, void* stream) {
     return pair_exchange(op->dtype, op->orbitals, op->n_orb, op->jbuf, out, op_n3(*op), s);
   }
   return poisson_run(op->pp->p, a, EPI_ACC, true, nullptr, s);
+}
+
+extern "C" int gato_op_tune(gato_op_t op, int block_epilogue) {
+  if (!op || block_epilogue < 0 || block_epilogue > 2)
+    return fail(GATO_EBADARG, "gato_op_tune: block epilogue must be 0, 1 or 2");
+  op->block_epi = block_epilogue;
+  return GATO_OK;
 }
 
 extern "C" int gato_op_energy_terms(gato_op_t op, const void* V_ext, double* terms, void* stream) {

@@ -18,6 +18,7 @@ struct gato_operator {
   void* rho = nullptr;          // N^3 density scratch for the energy terms
   void* jbuf = nullptr;         // pair potentials J_ij of the block apply
   size_t jbuf_bytes = 0;
+  int block_epi = 0;            // block apply epilogue: 0 auto, 1 J fields + pair pass, 2 fused
 };
 
 namespace gato {

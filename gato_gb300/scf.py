@@ -70,6 +70,12 @@ class Operator:
             _lib._lib.gato_op_destroy(h)
             self.handle = None
 
+    block_epilogue = 0   # 0 auto, 1 J fields + pair pass, 2 fused accumulation (see gato_op_tune)
+
+    def tune(self, block_epilogue: int):
+        _lib.call("gato_op_tune", self.handle, int(block_epilogue))
+        self.block_epilogue = int(block_epilogue)
+
     def set_potential(self, V: torch.Tensor | None):
         self._keep["V"] = V
         _lib.call("gato_op_set_potential", self.handle, C.c_void_p(V.data_ptr() if V is not None else None))

@@ -173,6 +173,10 @@ int gato_op_destroy(gato_op_t op);
 int gato_op_set_potential(gato_op_t op, const void* V);
 int gato_op_set_nonlocal(gato_op_t op, gato_nonlocal_t nl);
 int gato_op_set_exchange(gato_op_t op, gato_poisson_t plan, const void* orbitals, int n_orb);
+/* Block-apply epilogue: 0 = auto, 1 = J_ij fields then one pair pass, 2 =
+ * accumulate every output in the z-inverse epilogue. No reference
+ * counterpart (a tuning knob of this library, set by the autotuner).      */
+int gato_op_tune(gato_op_t op, int block_epilogue);
 /* out = F in, one vector.                                                  */
 int gato_op_apply(gato_op_t op, const void* in, void* out, void* stream);
 /* out_i = F phi_i for the operator's own n_orb orbitals, with the

@@ -302,6 +302,17 @@ def test_block_fock_golden(dtype):
     assert rel_err(one, GOLD["water_block_fock"][2]) < (1e-11 if dtype == torch.float64 else 3e-5)
 
 
+@pytest.mark.parametrize("epilogue", [1, 2])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_block_fock_epilogues(dtype, epilogue):
+    """Both block-apply epilogues (J fields + pair pass, fused accumulation) against the golden block."""
+    _, F, _ = _water_fock(dtype)
+    op = F._gato_operator(dtype, allow_generic=True)
+    op.tune(epilogue)
+    got = host(op.apply_block())
+    assert rel_err(got, GOLD["water_block_fock"]) < (1e-11 if dtype == torch.float64 else 3e-5)
+
+
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_energy_terms_golden(dtype):
     from gato_gb300.scf import decompose_rhf_energy
