@@ -199,6 +199,11 @@ def e2e_pipelined(st, g, host_in, steps):
     outs.append(torch.empty_like(st["out"]))
     hosts = [torch.empty_like(host_in).pin_memory() for _ in range(2)]
     ev = lambda: torch.cuda.Event()   # noqa: E731
+    try:   # each operator's block apply as a graph replay, as in the headline
+        graphs = [op.block_graph(o) for op, o in zip(ops, outs)]
+        steps_fn = [g.replay for g in graphs]
+    except Exception:
+        steps_fn = [lambda b=b: ops[b].apply_block(outs[b]) for b in range(2)]
 
     def run(n):
         done = [None, None]   # compute of the buffer's previous step (frees its input and output)
@@ -218,7 +223,7 @@ def e2e_pipelined(st, g, host_in, steps):
             comp.wait_event(loaded[k])
             if k >= 2:
                 comp.wait_event(dl[b])   # the buffer's previous result is home
-            ops[b].apply_block(outs[b])
+            steps_fn[b]()
             done[b] = ev()
             done[b].record(comp)
             with torch.cuda.stream(down):
@@ -363,10 +368,24 @@ def run_gato(args):
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
+    # the step as direct launches, then as a replay of the same launches captured once in a CUDA graph
+    direct = timed(lambda: op32.apply_block(s32["out"]), args.steps, 0)
+    graph = None
+    try:
+        l0 = _lib.launch_count()
+        graph = op32.block_graph(s32["out"])
+        per_step = (_lib.launch_count() - l0) // 2      # one warm-up run and the captured run
+    except Exception as exc:   # capture refused: the direct launches are the step
+        graph_error = f"{type(exc).__name__}: {exc}"
+        per_step = None
     l0 = _lib.launch_count()
     with ClockSampler(local) as clk:
-        times = timed(lambda: op32.apply_block(s32["out"]), args.steps, 0)
-    launches = (_lib.launch_count() - l0) // max(args.steps, 1) * args.steps
+        if graph is not None:
+            times = timed(graph.replay, args.steps, 3)
+            launches = per_step * args.steps
+        else:
+            times = timed(lambda: op32.apply_block(s32["out"]), args.steps, 0)
+            launches = (_lib.launch_count() - l0) // max(args.steps, 1) * args.steps
     t_local = sum(times)
     t_max = t_local
     if world > 1:
@@ -464,6 +483,10 @@ def run_gato(args):
                         "and result (no L2 flush: the step streams ~1 GB of spectral buffers)",
                 "serial_value": e2e_serial},
         "gpu_launches": int(launches),
+        "cuda_graph": ({"used": True, "kernels_per_step": per_step,
+                        "direct_launch_value": world * args.steps / sum(direct)} if graph is not None
+                       else {"used": False, "error": graph_error,
+                             "direct_launch_value": world * args.steps / sum(direct)}),
         "roofline": {"kernel": "k_cols<float2, FMI> (x FFT, kernel multiply, inverse x FFT)", "bound": "hbm",
                      "achieved": bytes_x / tx_avg / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": bytes_x / tx_avg / 1e9 / peak,

@@ -105,6 +105,26 @@ class Operator:
         _lib.call("gato_op_apply_block", self.handle, C.c_void_p(out.data_ptr()), C.c_void_p(_lib.stream()))
         return out
 
+    def block_graph(self, out: torch.Tensor) -> torch.cuda.CUDAGraph:
+        """``apply_block(out)`` captured once as a CUDA graph; ``replay()`` re-runs its launches.
+
+        The graph holds the addresses of the orbitals, potential, projectors, plan
+        buffers and ``out``: their values may change between replays, their
+        storage may not, and a later ``set_*``/``tune`` call (or a plan or stencil
+        tuning change) needs a new graph. A warm-up run first lets the operator
+        allocate its pair-potential buffer, so nothing allocates inside the graph;
+        the block apply uses no per-stream scratch. Replays on one stream at a
+        time: the plan's spectral buffers and the projector object are shared."""
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            self.apply_block(out)
+        torch.cuda.current_stream().wait_stream(side)
+        with torch.cuda.graph(g, stream=side, capture_error_mode="relaxed"):
+            self.apply_block(out)
+        return g
+
     def energy_terms(self, V_ext: torch.Tensor | None) -> torch.Tensor:
         """(kinetic, v_ext, v_nl, hartree, exchange) as a float64 CUDA tensor."""
         terms = torch.empty(5, dtype=torch.float64, device=_lib.require_cuda())

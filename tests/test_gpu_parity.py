@@ -314,6 +314,28 @@ def test_block_fock_epilogues(dtype, epilogue):
 
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_block_fock_graph_replay(dtype):
+    """The CUDA-graph replay of the block apply matches direct launches, and follows new orbital values
+    written into the same storage."""
+    _, F, _ = _water_fock(dtype)
+    op = F._gato_operator(dtype, allow_generic=True)
+    orb = op._keep["orb"]
+    out = torch.empty_like(orb)
+    g = op.block_graph(out)
+    ref = op.apply_block().clone()
+    out.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref)
+    orb.mul_(0.9)          # new values, same storage: F depends on them through the exchange term
+    ref2 = op.apply_block().clone()
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out, ref2)
+    assert not torch.equal(ref, ref2)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_energy_terms_golden(dtype):
     from gato_gb300.scf import decompose_rhf_energy
     g, F, _ = _water_fock(dtype)
