@@ -357,6 +357,135 @@ __global__ void __launch_bounds__(kBulkThreads)
   }
 }
 
+// Vector-major variant of k_gemv_t_bulk for blocks whose range spans at most
+// kVmChunks chunks: the producer streams item t = k * nch + c (all chunks of
+// vector k, then vector k + 1), each consumer thread keeps w for every chunk
+// of the range in registers, accumulates vector k over its chunks and reduces
+// it across the warp once, with a plain store of the warp's partial. The
+// chunk-major kernel instead reduces every item and adds it to shared memory
+// in FP64, a dependent FP64 step per item on GB300's narrow FP64 pipe.
+constexpr int kVmChunks = 4;
+
+template <typename T>
+__device__ __forceinline__ void bulk_producer_vm(const T* V, int64_t ld, int nk, int64_t lo, int64_t hi,
+                                                 int nch, T* stage, uint64_t* full, uint64_t* empty,
+                                                 volatile int* abort_v, int* err) {
+  using G = BulkGeom<T>;
+  const int items = nk * nch;
+  int t = 0;
+  for (int k = 0; k < nk && !*abort_v; ++k)
+    for (int c = 0; c < nch; ++c, ++t) {
+      const int sl = t % kBulkStages;
+      if (t >= kBulkStages &&
+          !mbar_wait_bounded(&empty[sl], (uint32_t)(((t / kBulkStages) - 1) & 1), err, 105)) {
+        *abort_v = 1;
+        break;
+      }
+      if (*abort_v) break;
+      const int64_t base = lo + (int64_t)c * G::CH;
+      const int64_t cnt = hi - base < G::CH ? hi - base : G::CH;
+      const uint32_t bytes = (uint32_t)(cnt * sizeof(T));
+      mbar_expect_tx(&full[sl], bytes);
+      bulk_load(stage + (size_t)sl * G::CH, V + (int64_t)k * ld + base, bytes, &full[sl]);
+    }
+  (void)items;
+  if (*abort_v)   // let the copies in flight land (bounded) before the block exits
+    for (int p = t > kBulkStages ? t - kBulkStages : 0; p < t; ++p)
+      mbar_wait_bounded(&full[p % kBulkStages], (uint32_t)((p / kBulkStages) & 1), err, 106);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBulkThreads, 3)
+    k_gemv_t_vm(const T* __restrict__ V, int64_t ld, int nk, const T* __restrict__ W, Pre<T> pre,
+                int64_t n, double* part, int* err) {
+  using G = BulkGeom<T>;
+  using V4 = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  extern __shared__ __align__(128) unsigned char smb[];
+  T* stage = reinterpret_cast<T*>(smb);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smb + (size_t)kBulkStages * G::CH * sizeof(T));
+  uint64_t* empty = full + kBulkStages;
+  double* wacc = reinterpret_cast<double*>(empty + kBulkStages);   // [warp][k]
+  __shared__ int abort_flag;
+  volatile int* abort_v = &abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int64_t lo, hi;
+  block_range(n, lo, hi);
+  const int nch = hi > lo ? (int)((hi - lo + G::CH - 1) / G::CH) : 0;   // <= kVmChunks (host-checked)
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kBulkStages; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], kBulkWarps);
+    }
+    abort_flag = 0;
+    fence_barrier_init();
+  }
+  for (int i = threadIdx.x; i < kBulkWarps * nk; i += blockDim.x) wacc[i] = 0.0;
+  __syncthreads();
+  if (warp == kBulkWarps) {
+    if (lane == 0) bulk_producer_vm<T>(V, ld, nk, lo, hi, nch, stage, full, empty, abort_v, err);
+  } else {
+    const int ct = threadIdx.x;
+    T sc[2];
+    pre_scalars(pre, sc);
+    // w for every chunk of the range; elements past hi are zero
+    T w[kVmChunks][G::EPT];
+    int lim[kVmChunks];   // valid elements of chunk c
+#pragma unroll
+    for (int c = 0; c < kVmChunks; ++c) {
+      const int64_t base = lo + (int64_t)c * G::CH;
+      lim[c] = c < nch ? (int)(hi - base < G::CH ? hi - base : G::CH) : 0;
+#pragma unroll
+      for (int g = 0; g < G::GRP; ++g)
+#pragma unroll
+        for (int u = 0; u < G::VEC; ++u) {
+          const int li = G::idx(ct, g, u);
+          w[c][g * G::VEC + u] = li < lim[c] ? pre_load(W, pre, sc, base + li) : (T)0;
+        }
+    }
+    int t = 0;
+    bool ok = true;
+    for (int k = 0; k < nk && ok; ++k) {
+      T sk = (T)0;
+#pragma unroll
+      for (int c = 0; c < kVmChunks; ++c) {
+        if (c >= nch) break;
+        if (!bulk_wait(full, t, abort_v, err)) {
+          ok = false;
+          break;
+        }
+        const T* st = stage + (size_t)(t % kBulkStages) * G::CH;
+        T v[G::EPT];
+#pragma unroll
+        for (int g = 0; g < G::GRP; ++g) {
+          const V4 q = *reinterpret_cast<const V4*>(st + G::idx(ct, g, 0));
+          const T* qe = reinterpret_cast<const T*>(&q);
+#pragma unroll
+          for (int u = 0; u < G::VEC; ++u) v[g * G::VEC + u] = qe[u];
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[t % kBulkStages]);
+        ++t;
+        const bool whole = lim[c] == G::CH;
+#pragma unroll
+        for (int g = 0; g < G::GRP; ++g)
+#pragma unroll
+          for (int u = 0; u < G::VEC; ++u)
+            if (whole || G::idx(ct, g, u) < lim[c]) sk = fma(v[g * G::VEC + u], w[c][g * G::VEC + u], sk);
+      }
+      if (!ok) break;
+      const double d = warp_total<T>(sk);
+      if (lane == 0) wacc[warp * nk + k] = d;
+    }
+  }
+  __syncthreads();
+  if (*abort_v) return;
+  for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+    double sum = 0.0;
+    for (int wp = 0; wp < kBulkWarps; ++wp) sum += wacc[wp * nk + k];
+    part[(int64_t)k * gridDim.x + blockIdx.x] = sum;
+  }
+}
+
 // k_gemv_n with bulk streaming: W <- W - pre - sum_k c_k v_k, norm partial
 // part[block]; the correction accumulates in FP32 as in k_gemv_n<T, float>.
 template <typename T>
@@ -826,6 +955,15 @@ int gemv_t_bulk(const T* V, int64_t ld, int nk, const T* W, const Pre<T>& pre, i
   const size_t sm = (size_t)kBulkStages * BulkGeom<T>::CH * sizeof(T) + 2 * kBulkStages * sizeof(uint64_t) +
                     (size_t)kBulkWarps * nk * sizeof(double);
   if (sm > 100 * 1024) return fail(GATO_EUNSUPPORTED, "lanczos: Krylov dimension too large for the bulk sweep");
+  // the block range of block_range(): chunks per block decide the variant
+  int64_t per = (n + nblk - 1) / nblk;
+  per = (per + 31) / 32 * 32;
+  if ((per + BulkGeom<T>::CH - 1) / BulkGeom<T>::CH <= kVmChunks) {
+    GATO_TRY(bulk_smem_attr(k_gemv_t_vm<T>, sm));
+    k_gemv_t_vm<T><<<nblk, kBulkThreads, sm, s>>>(V, ld, nk, W, pre, n, part, device_error_word());
+    GATO_LAUNCH_TRY();
+    return GATO_OK;
+  }
   GATO_TRY(bulk_smem_attr(k_gemv_t_bulk<T>, sm));
   k_gemv_t_bulk<T><<<nblk, kBulkThreads, sm, s>>>(V, ld, nk, W, pre, n, part, device_error_word());
   GATO_LAUNCH_TRY();
