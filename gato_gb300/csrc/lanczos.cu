@@ -498,7 +498,7 @@ __global__ void __launch_bounds__(kBulkThreads)
   T* stage = reinterpret_cast<T*>(smb);
   uint64_t* full = reinterpret_cast<uint64_t*>(smb + (size_t)kBulkStages * G::CH * sizeof(T));
   uint64_t* empty = full + kBulkStages;
-  double* cs = reinterpret_cast<double*>(empty + kBulkStages);
+  float* cs = reinterpret_cast<float*>(empty + kBulkStages);   // coefficients rounded once to FP32
   __shared__ double sh[32];
   __shared__ int abort_flag;
   volatile int* abort_v = &abort_flag;
@@ -515,7 +515,7 @@ __global__ void __launch_bounds__(kBulkThreads)
     abort_flag = 0;
     fence_barrier_init();
   }
-  for (int i = threadIdx.x; i < nk; i += blockDim.x) cs[i] = c_in[i];
+  for (int i = threadIdx.x; i < nk; i += blockDim.x) cs[i] = (float)c_in[i];
   __syncthreads();
   Acc<T> acc;
   if (warp == kBulkWarps) {
@@ -551,7 +551,7 @@ __global__ void __launch_bounds__(kBulkThreads)
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[t % kBulkStages]);
-      const float ck = (float)cs[k];
+      const float ck = cs[k];
 #pragma unroll
       for (int e = 0; e < G::EPT; ++e) corr[e] = fmaf(ck, (float)v[e], corr[e]);
       if (k == nk - 1) {

@@ -605,37 +605,65 @@ bool poisson_j_supported(const PoissonPlan& pl) {
 }
 
 namespace {
-// out_a -= sum over pairs (a, b) of phi_b J_ab (each J read once).
-template <typename T, int NORB>
+// out_a -= sum over pairs (a, b) of phi_b J_ab (each J read once). V is the
+// element group a thread moves per field: a 16-byte vector where every field
+// starts on a 16-byte boundary and n3 divides into vectors, else one element.
+template <typename T, int NORB, int V>
 __global__ void k_pair_exchange(const T* __restrict__ orb, const T* __restrict__ J, T* out, int64_t n3) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n3;
+  using VT = typename std::conditional<V == 1, T,
+             typename std::conditional<sizeof(T) == 4, float4, double2>::type>::type;
+  const int64_t nv = n3 / V;
+  const VT* o4 = reinterpret_cast<const VT*>(orb);
+  const VT* j4 = reinterpret_cast<const VT*>(J);
+  VT* r4 = reinterpret_cast<VT*>(out);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv;
        i += (int64_t)gridDim.x * blockDim.x) {
-    T phi[NORB], acc[NORB];
+    VT phiv[NORB];
+    T acc[NORB][V];
 #pragma unroll
     for (int a = 0; a < NORB; ++a) {
-      phi[a] = orb[(int64_t)a * n3 + i];
-      acc[a] = (T)0;
+      phiv[a] = o4[(int64_t)a * nv + i];
+#pragma unroll
+      for (int u = 0; u < V; ++u) acc[a][u] = (T)0;
     }
     int k = 0;
 #pragma unroll
     for (int a = 0; a < NORB; ++a)
 #pragma unroll
       for (int b = a; b < NORB; ++b, ++k) {
-        const T j = J[(int64_t)k * n3 + i];
-        acc[a] += phi[b] * j;
-        if (b != a) acc[b] += phi[a] * j;
+        const VT jv = j4[(int64_t)k * nv + i];
+        const T* j = reinterpret_cast<const T*>(&jv);
+        const T* pa = reinterpret_cast<const T*>(&phiv[a]);
+        const T* pb = reinterpret_cast<const T*>(&phiv[b]);
+#pragma unroll
+        for (int u = 0; u < V; ++u) {
+          acc[a][u] += pb[u] * j[u];
+          if (b != a) acc[b][u] += pa[u] * j[u];
+        }
       }
 #pragma unroll
-    for (int a = 0; a < NORB; ++a) out[(int64_t)a * n3 + i] -= acc[a];
+    for (int a = 0; a < NORB; ++a) {
+      VT r = r4[(int64_t)a * nv + i];
+      T* re = reinterpret_cast<T*>(&r);
+#pragma unroll
+      for (int u = 0; u < V; ++u) re[u] -= acc[a][u];
+      r4[(int64_t)a * nv + i] = r;
+    }
   }
 }
 
 template <typename T>
 int pair_exchange_t(const T* orb, int n, const T* J, T* out, int64_t n3, cudaStream_t s) {
-  const unsigned g = grid_for(n3, 256, 152 * 8);
+  constexpr int VEC = 16 / (int)sizeof(T);
+  const bool vec = n3 % VEC == 0 && (uintptr_t)orb % 16 == 0 && (uintptr_t)J % 16 == 0 &&
+                   (uintptr_t)out % 16 == 0;
+  const unsigned g = grid_for(vec ? n3 / VEC : n3, 256, 152 * 8);
   switch (n) {
-#define GATO_PX(NN) \
-  case NN: k_pair_exchange<T, NN><<<g, 256, 0, s>>>(orb, J, out, n3); break;
+#define GATO_PX(NN)                                                          \
+  case NN:                                                                   \
+    if (vec) k_pair_exchange<T, NN, VEC><<<g, 256, 0, s>>>(orb, J, out, n3); \
+    else k_pair_exchange<T, NN, 1><<<g, 256, 0, s>>>(orb, J, out, n3);       \
+    break;
     GATO_PX(1) GATO_PX(2) GATO_PX(3) GATO_PX(4) GATO_PX(5) GATO_PX(6) GATO_PX(7) GATO_PX(8)
 #undef GATO_PX
     default: return fail(GATO_EUNSUPPORTED, "pair exchange: at most 8 orbitals");

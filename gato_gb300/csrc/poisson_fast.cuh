@@ -208,10 +208,10 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   const TwPrefetch<T2, R1 * TwRow<T2, R2>::S, NT> twp(tw);
   const int64_t row0 = (int64_t)blockIdx.x * L;
   const int64_t nrows = (int64_t)N * N;
-  // staging: up to 32 loads in flight per thread per batch (one batch for four
-  // inputs of 8 rows), so the row block costs one global round trip
+  // staging: 8 loads in flight per thread per batch (measured faster than one
+  // batch of 32 at 128^3: 53 against 69 us)
   const int nel = ri.nin * L * N;
-  constexpr int B = 32;
+  constexpr int B = 8;
   for (int base = 0; base < nel; base += B * NT) {
     T v[B];
 #pragma unroll
