@@ -338,10 +338,11 @@ def run_gato(args):
     from gato_gb300.autotune import tune_block_epilogue
     for name, st in (("mixed", s32), ("fp64", s64)):
         step = lambda st=st: st["op"].apply_block(st["out"])  # noqa: E731
-        best = tune_plan(st["plan"], step, key="block")
+        best = tune_plan(st["plan"], step, key="block", engines=(0, 2))
         epi = tune_block_epilogue(st["op"], step, key="block")
         tuned[name] = {"group": best["group"], "engine": best["engine"],
-                       "candidates_ms": {str(c["group"]): round(c["ms"], 4) for c in best["candidates"]},
+                       "candidates_ms": {f'{c["engine"]}:{c["group"]}': round(c["ms"], 4)
+                                         for c in best["candidates"]},
                        "block_epilogue": epi["epilogue"],
                        "epilogue_ms": {str(c["epilogue"]): round(c["ms"], 4) for c in epi["candidates"]}}
 
@@ -673,7 +674,7 @@ def run_profile(args):
     el = water_hgh_elements()
     fields = torch.tensor(orbs, device="cuda").to(dtype).contiguous()
     plan = get_plan(N, h, h / 2, dtype, pair_fields(N_OCC))
-    set_plan(plan, plan.max_fields)
+    set_plan(plan, plan.max_fields, args.engine)
     op = Operator(g, dtype, 4, "dirichlet")
     op.set_potential((hgh_local_potential(nuc, el, g, dtype) + plan.potential(_density_fields(fields))).contiguous())
     op.set_nonlocal(nonlocal_for(nuc, el, g, dtype))
@@ -721,6 +722,8 @@ def main():
     ap.add_argument("--profile", default=None, choices=["block", "matvec", "scf"],
                     help="run only the block / matvec Fock apply or two SCF iterations (for ncu captures)")
     ap.add_argument("--profile-dtype", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--engine", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="FFT engine of the --profile run (see gato_poisson_tune)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -35,9 +35,9 @@ int cols<T>(int M, int mode, const T2* in, T2* out, const ColGeom& g, int outer,
 }
 
 template <>
-int rows_fwd<T>(int M, const PassArgs& a, int f0, int nfg, T2* S1, const T2* tw, cudaStream_t s) {
+int rows_fwd<T>(int M, const PassArgs& a, int f0, int nfg, T2* S1, const T2* tw, int multi, cudaStream_t s) {
 #define X(MM, A, B, L32, L64) \
-  case MM: return Launch<T, A, B, kF32 ? L32 : L64>::rows_fwd(a, f0, nfg, S1, tw, s);
+  case MM: return Launch<T, A, B, kF32 ? L32 : L64>::rows_fwd(a, f0, nfg, S1, tw, multi, s);
   switch (M) { GATO_FAST_SHAPES(X) }
 #undef X
   return kNotHandled;

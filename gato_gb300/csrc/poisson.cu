@@ -296,7 +296,7 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
   const T2* tw2 = (const T2*)pl.tw2;   // the register engine's per-row stage twiddles
   T2* S1 = (T2*)pl.S1;
   T2* S2 = (T2*)pl.S2;
-  const int Lf = pl.engine == 0 ? fast::rows_L<T>(M) : 0;   // register engine, 0: generic
+  const int Lf = pl.engine != 1 ? fast::rows_L<T>(M) : 0;   // register engine, 0: generic
   const int Lr = pick_L<T2>(M, 0, sizeof(T) == 4 ? 16 : 8);
   const int Li = pick_L<T2>(M, (size_t)args.nout * N * sizeof(T), sizeof(T) == 4 ? 16 : 8);
   const size_t sm_r = fft_smem<T2>(M, Lr);
@@ -323,7 +323,8 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
     const int64_t sstride = (int64_t)ngroups * nblk_i;
     if (Lf > 0) {
       // register-resident two-pass engine
-      GATO_TRY(fast::rows_fwd<T>(M, args, f0, nfg, S1, tw2, s));
+      // engine 0: multi-field z forward from two fields, 2: never, 3: from three
+      GATO_TRY(fast::rows_fwd<T>(M, args, f0, nfg, S1, tw2, pl.engine == 2 ? 0 : (pl.engine == 3 ? 1 : 2), s));
       GATO_TRY(fast::cols<T>(M, COL_FWD, S1, S2, gy, N, nfg, tw2, nullptr, pl.H, s));
       GATO_TRY(fast::cols<T>(M, COL_FMI, S2, S2, gx, M, nfg, tw2, (const T*)pl.ghat, pl.H, s));
       GATO_TRY(fast::cols<T>(M, COL_INV, S2, S1, gyi, N, nfg, tw2, nullptr, pl.H, s));
@@ -563,7 +564,7 @@ extern "C" int gato_poisson_stage(gato_poisson_t plan, int stage, int nf, void* 
     using T2 = std::remove_pointer_t<decltype(S1)>;
     using T = std::remove_const_t<std::remove_pointer_t<decltype(ghat)>>;
     const int mode = stage == 1 ? COL_FWD : (stage == 2 ? COL_FMI : COL_INV);
-    if (pl.engine == 0 && fast::rows_L<T>(M) > 0) {
+    if (pl.engine != 1 && fast::rows_L<T>(M) > 0) {
       ColGeom g1{nrows * M, (int64_t)N * M * M, (int64_t)N * M, (int64_t)M * M, M, M, M, N, M};
       ColGeom g2{(int64_t)N * M * M, (int64_t)N * M * M, M, M, (int64_t)M * M, (int64_t)M * M, M, N, N};
       ColGeom g3{(int64_t)N * M * M, nrows * M, (int64_t)M * M, (int64_t)N * M, M, M, M, M, N};
@@ -589,9 +590,12 @@ extern "C" int gato_poisson_stage(gato_poisson_t plan, int stage, int nf, void* 
 }
 
 // Tuning knobs: fields per launch group (1..max_fields, 0 = all) and the FFT
-// engine (0: register-resident two-pass kernels where M has one, 1: generic).
+// engine (0: register-resident two-pass kernels where M has one, with the
+// multi-field z forward for groups of two or more fields; 1: generic; 2: the
+// register kernels with one z-forward CTA per field; 3: the register kernels
+// with the multi-field z forward from three fields).
 extern "C" int gato_poisson_tune(gato_poisson_t plan, int group, int engine) {
-  if (!plan || group < 0 || group > plan->p.max_fields || engine < 0 || engine > 1)
+  if (!plan || group < 0 || group > plan->p.max_fields || engine < 0 || engine > 3)
     return fail(GATO_EBADARG, "gato_poisson_tune: bad arguments");
   plan->p.group = group;
   plan->p.engine = engine;
@@ -600,7 +604,7 @@ extern "C" int gato_poisson_tune(gato_poisson_t plan, int group, int engine) {
 
 namespace gato {
 bool poisson_j_supported(const PoissonPlan& pl) {
-  if (pl.engine != 0) return false;
+  if (pl.engine == 1) return false;
   return (pl.dtype == GATO_F64 ? fast::rows_L<double>(pl.M) : fast::rows_L<float>(pl.M)) > 0;
 }
 

@@ -85,7 +85,7 @@ int cols(int M, int mode, const typename Cplx<T>::type* in, typename Cplx<T>::ty
          int H, cudaStream_t s);
 template <typename T>
 int rows_fwd(int M, const PassArgs& a, int f0, int nfg, typename Cplx<T>::type* S1,
-             const typename Cplx<T>::type* tw, cudaStream_t s);
+             const typename Cplx<T>::type* tw, int multi, cudaStream_t s);
 template <typename T>
 int rows_inv(int M, const PassArgs& a, int f0, int nfg, const typename Cplx<T>::type* S1,
              const typename Cplx<T>::type* tw, int accumulate, bool energy, double* partials,

@@ -3,6 +3,7 @@
 #pragma once
 #include "fft2.cuh"
 #include "poisson.cuh"
+#include "ptx.cuh"
 
 namespace gato {
 namespace fast {
@@ -195,19 +196,57 @@ struct RowsIn {
 // field. Stage-1 lanes read consecutive z of RMAX-lane lines, so a staged row
 // is padded to a multiple of 32 words plus RMAX (StageRow): the lines a warp
 // reads fall in disjoint bank ranges.
-template <typename T, int R1, int R2, int L>
+// BULK: one elected thread stages every row with a 1-D bulk copy
+// (cp.async.bulk, one mbarrier for the whole block, a bounded wait), so the
+// staging costs one round trip and no registers; used when every input is
+// 16-byte aligned, a row and a padded staged row are multiples of 16 bytes
+// and L divides the rows.
+// Otherwise the threads stage with batches of 8 loads each.
+template <typename T, int R1, int R2, int L, bool BULK>
 __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
     k_rows_fwd_multi(PassArgs args, RowsIn ri, int f0, int nfg, typename Cplx<T>::type* S1,
-                     const typename Cplx<T>::type* tw) {
+                     const typename Cplx<T>::type* tw, int* err) {
   using T2 = typename Cplx<T>::type;
   constexpr int M = R1 * R2, N = M / 2, NP = StageRow<R1, R2>::NP, RM = Shape<R1, R2>::RMAX, NT = L * RM;
   extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ __align__(8) uint64_t sbar;
   T2* buf = reinterpret_cast<T2*>(smraw);
   T2* tws = buf + L * RowBuf<R1, R2>::LS;
   T* stage = reinterpret_cast<T*>(tws + R1 * TwRow<T2, R2>::S);   // [slot][line][z], rows of NP
   const TwPrefetch<T2, R1 * TwRow<T2, R2>::S, NT> twp(tw);
   const int64_t row0 = (int64_t)blockIdx.x * L;
   const int64_t nrows = (int64_t)N * N;
+  if constexpr (BULK) {
+    __shared__ int s_misaligned;
+    if (threadIdx.x == 0) {
+      mbar_init(&sbar, 1);
+      fence_barrier_init();
+      // the host only picks this path for 16-byte aligned rows; re-check, and
+      // record an error instead of issuing a copy that would fault
+      int bad_align = (int)((smem_u32(stage) | (uint32_t)(NP * sizeof(T)) | (uint32_t)(N * sizeof(T))) & 15u);
+      for (int sl = 0; sl < ri.nin; ++sl)
+        bad_align |= (int)(reinterpret_cast<uintptr_t>(args.in[ri.idx[sl]]) & 15u);
+      s_misaligned = bad_align;
+      if (bad_align && err) atomicExch(err, 110);
+    }
+    __syncthreads();   // the barrier is initialised before anyone waits on it
+    if (s_misaligned) return;
+    if (threadIdx.x == 0) {
+      mbar_expect_tx(&sbar, (uint32_t)(ri.nin * L * N * sizeof(T)));
+      for (int sl = 0; sl < ri.nin; ++sl) {
+        const T* src = reinterpret_cast<const T*>(args.in[ri.idx[sl]]) + row0 * N;
+        for (int l = 0; l < L; ++l)
+          bulk_load(stage + (sl * L + l) * NP, src + (int64_t)l * N, (uint32_t)(N * sizeof(T)), &sbar);
+      }
+    }
+    twp.store(tws);
+    bool bad = false;
+    if (!mbar_wait_bounded(&sbar, 0, err, 108)) bad = true;
+    if (__syncthreads_or(bad)) {
+      if (threadIdx.x == 0) mbar_wait_bounded(&sbar, 0, err, 109);   // the copies still land
+      return;
+    }
+  } else {
   // staging: 8 loads in flight per thread per batch (measured faster than one
   // batch of 32 at 128^3: 53 against 69 us)
   const int nel = ri.nin * L * N;
@@ -232,6 +271,7 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   }
   twp.store(tws);
   __syncthreads();
+  }
   const int line = threadIdx.x / RM, j = threadIdx.x % RM;
   const int64_t r = row0 + line;
   for (int p = 0; p < nfg; ++p) {
@@ -274,8 +314,14 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
 // z inverse over every field of the group, then the epilogue. NO > 0: the
 // accumulation terms target outputs < NO, kept in registers (each thread owns
 // the R1/2 fixed elements z = j + R2 n1 of its row); NO == 0: energy mode.
+// FP32, one output, M = 256 fits 64 registers without spills: four CTAs per SM.
+template <typename T, int R1, int R2, int NO>
+constexpr int rows_inv_min_ctas() {
+  return (NO == 1 && sizeof(T) == 4 && R1 == 16 && R2 == 16) ? 4 : 1;
+}
+
 template <typename T, int R1, int R2, int L, int NO>
-__global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
+__global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX, (rows_inv_min_ctas<T, R1, R2, NO>()))
     k_rows_inv(PassArgs args, int f0, int nfg, const typename Cplx<T>::type* S1,
                const typename Cplx<T>::type* tw, int accumulate, double* partials,
                int64_t slot_stride) {
@@ -301,24 +347,30 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   for (int p = 0; p < nfg; ++p) {
     const FieldDesc& fd = args.f[f0 + p];
     // The epilogue's first field factor of each part (in[tc] of term 0, or the
-    // density in energy mode) does not depend on the transform: load it now so
-    // its latency overlaps the FFT instead of following it. A second term
-    // (block applies on the generic engine only) still loads in the epilogue.
+    // density in energy mode) does not depend on the transform. With several
+    // outputs (or energies) it is loaded now, so its latency overlaps the FFT;
+    // with one output it is loaded in the epilogue, which keeps the kernel at
+    // four CTAs per SM (64 registers). A second term (block applies on the
+    // generic engine only) always loads in the epilogue.
+    constexpr bool PREFETCH = ENERGY || NO > 1;
     T fac[EPT][2];
+    auto load_fac = [&]() {
 #pragma unroll
-    for (int e = 0; e < EPT; ++e) {
-      const int64_t gi = r * N + j + R2 * e;
+      for (int e = 0; e < EPT; ++e) {
+        const int64_t gi = r * N + j + R2 * e;
 #pragma unroll
-      for (int qq = 0; qq < 2; ++qq) {
-        const PartDesc& d = fd.p[qq];
-        if constexpr (ENERGY)
-          fac[e][qq] = (own && d.a >= 0) ? dens<T>(d, args.in, gi) : (T)0;
-        else
-          fac[e][qq] = (own && d.a >= 0 && d.nt > 0)
-                           ? (d.tc[0] >= 0 ? reinterpret_cast<const T*>(args.in[d.tc[0]])[gi] : (T)1)
-                           : (T)0;
+        for (int qq = 0; qq < 2; ++qq) {
+          const PartDesc& d = fd.p[qq];
+          if constexpr (ENERGY)
+            fac[e][qq] = (own && d.a >= 0) ? dens<T>(d, args.in, gi) : (T)0;
+          else
+            fac[e][qq] = (own && d.a >= 0 && d.nt > 0)
+                             ? (d.tc[0] >= 0 ? reinterpret_cast<const T*>(args.in[d.tc[0]])[gi] : (T)1)
+                             : (T)0;
+        }
       }
-    }
+    };
+    if constexpr (PREFETCH) load_fac();
     T2 X[R2];
     if (j < R1) {
       const T2* src = S1 + (int64_t)p * nrows * M + r * M + j;
@@ -333,6 +385,7 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
     if (j < R1) row_inv_stageA<T2, R1, R2>(buf, line, j, tws, X);
     __syncthreads();
     if (own) {
+      if constexpr (!PREFETCH) load_fac();
       T2 w[R1];
       row_inv_stageB<T2, R1, R2>(buf, line, j, w);
 #pragma unroll
@@ -464,10 +517,11 @@ struct Launch {
     GATO_LAUNCH_TRY();
     return GATO_OK;
   }
-  static int rows_fwd(const PassArgs& a, int f0, int nfg, T2* S1, const T2* tw, cudaStream_t s) {
-    // three or more fields over few distinct inputs: stage the inputs once per
-    // CTA (with two fields, as in the matvec exchange, the per-field kernel's
-    // higher occupancy wins: 36 against 46 us at 128^3)
+  // multi: 0 per-field CTAs, 1 multi-field CTAs from three fields up, 2 from two fields up
+  // (the default: with bulk staging the multi-field kernel wins at two fields too,
+  // 239 against 244 us for the 128^3 matvec)
+  static int rows_fwd(const PassArgs& a, int f0, int nfg, T2* S1, const T2* tw, int multi, cudaStream_t s) {
+    // several fields over few distinct inputs: stage the inputs once per CTA
     RowsIn ri;
     for (int i = 0; i < kMaxIn; ++i) ri.slot_of[i] = -1;
     auto use = [&](int idx) {
@@ -486,12 +540,24 @@ struct Launch {
     // field at once, so smaller CTAs give more of them and a shorter last wave
     constexpr int LM = L >= 16 ? L / 2 : L;
     const size_t stage_bytes = (size_t)ri.nin * LM * StageRow<R1, R2>::NP * sizeof(T);
-    if (nfg >= 3 && stage_bytes <= 48 * 1024) {
+    if (multi > 0 && nfg >= (multi == 2 ? 2 : 3) && stage_bytes <= 48 * 1024) {
       const size_t sm = (size_t)(LM * RowBuf<R1, R2>::LS + TWN) * sizeof(T2) + stage_bytes;
-      GATO_TRY(smem_attr(k_rows_fwd_multi<T, R1, R2, LM>, sm));
       const int64_t nrows = (int64_t)N * N;
-      k_rows_fwd_multi<T, R1, R2, LM><<<(unsigned)((nrows + LM - 1) / LM), LM * Shape<R1, R2>::RMAX, sm, s>>>(
-          a, ri, f0, nfg, S1, tw);
+      // a bulk copy needs 16-byte aligned source and destination rows and a
+      // size that is a multiple of 16 bytes (the padded staged row included)
+      bool bulk = nrows % LM == 0 && (N * sizeof(T)) % 16 == 0 &&
+                  (StageRow<R1, R2>::NP * sizeof(T)) % 16 == 0;
+      for (int i = 0; i < ri.nin; ++i) bulk = bulk && ((uintptr_t)a.in[ri.idx[i]] % 16) == 0;
+      const unsigned grid = (unsigned)((nrows + LM - 1) / LM);
+      if (bulk) {
+        GATO_TRY(smem_attr(k_rows_fwd_multi<T, R1, R2, LM, true>, sm));
+        k_rows_fwd_multi<T, R1, R2, LM, true><<<grid, LM * Shape<R1, R2>::RMAX, sm, s>>>(
+            a, ri, f0, nfg, S1, tw, device_error_word());
+      } else {
+        GATO_TRY(smem_attr(k_rows_fwd_multi<T, R1, R2, LM, false>, sm));
+        k_rows_fwd_multi<T, R1, R2, LM, false><<<grid, LM * Shape<R1, R2>::RMAX, sm, s>>>(
+            a, ri, f0, nfg, S1, tw, device_error_word());
+      }
       GATO_LAUNCH_TRY();
       return GATO_OK;
     }

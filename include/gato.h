@@ -139,7 +139,10 @@ int gato_hartree_energy(gato_poisson_t plan, const void* rho, double* E_dev, voi
 int gato_poisson_stage(gato_poisson_t plan, int stage, int nf, void* stream);
 /* Tuning (no reference counterpart): fields per launch group (0 = all of
  * max_fields) and FFT engine (0: register-resident two-pass kernels for
- * M in {32,48,64,80,96,128,160,192,256,320}, 1: generic Stockham).      */
+ * M in {32,48,64,80,96,128,160,192,256,320}, with the multi-field z
+ * forward for two or more fields; 1: generic Stockham; 2: the register
+ * kernels with one z-forward CTA per field; 3: the multi-field z forward
+ * from three fields).                                                    */
 int gato_poisson_tune(gato_poisson_t plan, int group, int engine);
 
 /* ---- scf.py ----------------------------------------------------------------

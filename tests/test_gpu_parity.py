@@ -314,6 +314,21 @@ def test_block_fock_epilogues(dtype, epilogue):
 
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_block_fock_per_field_z_forward(dtype):
+    """Engine 2 (one z-forward CTA per field) gives the golden block apply too."""
+    from gato_gb300.autotune import set_plan
+    _, F, _ = _water_fock(dtype)
+    op = F._gato_operator(dtype, allow_generic=True)
+    plan = op._keep["plan"]
+    set_plan(plan, 0, 2)
+    try:
+        got = host(op.apply_block())
+    finally:
+        set_plan(plan, 0, 0)
+    assert rel_err(got, GOLD["water_block_fock"]) < (1e-11 if dtype == torch.float64 else 3e-5)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_block_fock_graph_replay(dtype):
     """The CUDA-graph replay of the block apply matches direct launches, and follows new orbital values
     written into the same storage."""
