@@ -119,6 +119,19 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def job_rate(t_local: float, steps: int, world: int, dist=None, device=None):
+    """Whole-job rate of `world` replicas that each ran `steps` steps, the local one in `t_local`
+    seconds: the job took the slowest rank's time (an all-reduce MAX when world > 1), and every
+    rank's steps count. Returns (rate, job seconds)."""
+    t_max = t_local
+    if world > 1:
+        import torch
+        tt = torch.tensor([float(t_local)], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt)
+    return world * steps / t_max, t_max
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -387,13 +400,7 @@ def run_gato(args):
         else:
             times = timed(lambda: op32.apply_block(s32["out"]), args.steps, 0)
             launches = (_lib.launch_count() - l0) // max(args.steps, 1) * args.steps
-    t_local = sum(times)
-    t_max = t_local
-    if world > 1:
-        tt = torch.tensor([t_local], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt)
-    value = world * args.steps / t_max
+    value, t_max = job_rate(sum(times), args.steps, world, dist, dev)
 
     # ---- plain FP64 and matvec rates ----------------------------------------------
     k64 = max(2, args.steps // 4)
@@ -455,7 +462,7 @@ def run_gato(args):
         host_out.copy_(s32["out"], non_blocking=True)
     te = timed(e2e_step, args.steps, 2)
     e2e_serial = world * args.steps / sum(te)
-    e2e_val = world * args.steps / e2e_pipelined(s32, g, host_in, args.steps)
+    e2e_val, _ = job_rate(e2e_pipelined(s32, g, host_in, args.steps), args.steps, world, dist, dev)
 
     if rank != 0:
         if world > 1:
