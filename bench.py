@@ -535,7 +535,7 @@ def run_workload(args):
 
     from gato_gb300.grid import Grid3D
     out = {"workload": args.workload}
-    if args.workload == "c5":
+    if args.workload == "batch48":
         # 48 seeded systems (H2 / LiH / HCl / H2O, 64^3..160^3, h 0.2..0.3), mixed precision,
         # concurrent streams vs one stream, FP64 continuation checks on the grids <= 96^3
         from gato_gb300.batch import draw_systems, fp64_check, solve_batch, summarize
@@ -543,7 +543,7 @@ def run_workload(args):
         res, wall = solve_batch(specs, precision="mixed", streams=args.streams, max_iters=80, tol=1e-7)
         out["concurrent"] = summarize(res, wall)
         out["concurrent"]["streams"] = args.streams
-        if args.c5_sequential:
+        if args.batch_sequential:
             res1, wall1 = solve_batch(specs, precision="mixed", streams=1, max_iters=80, tol=1e-7)
             out["sequential_wall_s"] = wall1
             out["concurrency_speedup"] = wall1 / wall
@@ -559,7 +559,7 @@ def run_workload(args):
                               "per_system": checks}
         print(json.dumps(out), flush=True)
         return
-    if args.workload == "c1":
+    if args.workload == "hydrogen64":
         # hydrogen 64^3, L = 20, 7-point Laplacian, softened Coulomb a = 0.1, Lanczos m = 80, K = 1
         from gato_gb300.hamiltonian import Hamiltonian
         from gato_gb300.potentials import softened_coulomb
@@ -573,7 +573,7 @@ def run_workload(args):
             res, dt_s = _sync_time(lambda: lanczos(H, p, 80, 1))
             out[prec] = {"E0": float(res.eigenvalues[0]), "lanczos_s": dt_s}
         out["abs_dE0"] = abs(out["mixed"]["E0"] - out["fp64"]["E0"])
-    elif args.workload == "c2":
+    elif args.workload == "helium96":
         # helium RHF 96^3, L = 16, Z = 2, softening 0.1, Gaussian + 1e-3 noise, mixing 0.5, tol 1e-8
         from gato_gb300.potentials import softened_coulomb
         from gato_gb300.scf import scf_rhf
@@ -587,7 +587,7 @@ def run_workload(args):
                                               precision=prec))
             out[prec] = {"E": r.energy, "iters": r.n_iters, "converged": r.converged, "scf_s": t}
         out["abs_dE"] = abs(out["mixed"]["E"] - out["fp64"]["E"])
-    elif args.workload in ("c3", "c4"):
+    elif args.workload in ("water128", "water-geomopt"):
         from gato_gb300.physics.water import (bo_energy, hellmann_feynman_force, optimize_water_geometry,
                                               solve_rhf_at_geometry, water_hgh_elements, water_initial_geometry)
         from gato_gb300.scf import to_fields
@@ -595,7 +595,7 @@ def run_workload(args):
         g = Grid3D(N, N * h)
         el = water_hgh_elements()
         rng = np.random.default_rng(11)
-        if args.workload == "c3":
+        if args.workload == "water128":
             nuc = water_initial_geometry(1.81, 104.5)
             nuc = type(nuc)(nuc.positions + torch.tensor(rng.uniform(-0.05, 0.05, (3, 3))), nuc.charges)
             # the mixed SCF's energy noise floor is ~1e-8..1e-7 Ha (FP64 energies of orbitals from the
@@ -713,10 +713,13 @@ def run_profile(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--streams", type=int, default=8, help="concurrent streams of the c5 batch")
-    ap.add_argument("--c5-sequential", type=int, default=1, help="also time the c5 batch on one stream")
-    ap.add_argument("--workload", default=None, choices=["c1", "c2", "c3", "c4", "c5"],
-                    help="run a configuration workload instead of the headline metric")
+    ap.add_argument("--streams", type=int, default=8, help="concurrent streams of the 48-system batch")
+    ap.add_argument("--batch-sequential", type=int, default=1, help="also time the 48-system batch on one stream")
+    ap.add_argument("--workload", default=None,
+                    choices=["hydrogen64", "helium96", "water128", "water-geomopt", "batch48"],
+                    help="run one of the end-to-end workloads instead of the headline metric: hydrogen 64^3 "
+                         "Lanczos, helium 96^3 SCF, water 128^3 SCF, water geometry optimisation, "
+                         "48 mixed-size systems")
     ap.add_argument("--fp64-iters", type=int, default=3)
     ap.add_argument("--geom-steps", type=int, default=60)
     ap.add_argument("--fd-every", type=int, default=20)

@@ -1,13 +1,13 @@
-"""End-to-end checks of the benchmark configurations on the GPU.
+"""End-to-end checks of the benchmark workloads on the GPU.
 
-config 1: hydrogen, 64^3, L = 20, 7-point Laplacian, softened Coulomb (a = 0.1), Lanczos m = 80 from a
-          seeded uniform start -> E0 and psi0 against the FP64 oracle.
-config 2: helium RHF SCF, 96^3, L = 16, 13-point Laplacian, Z = 2, softening 0.1 for V_ext and the
+hydrogen: 64^3, L = 20, 7-point Laplacian, softened Coulomb (a = 0.1), Lanczos m = 80 from a seeded
+          uniform start -> E0 and psi0 against the FP64 oracle.
+helium:   RHF SCF, 96^3, L = 16, 13-point Laplacian, Z = 2, softening 0.1 for V_ext and the
           Hartree/exchange kernel, Gaussian + 1e-3 noise start, mixing 0.5, tol 1e-8, <= 30 iterations:
           FP64 path against the oracle iteration by iteration, mixed against FP64 at convergence.
-config 3: H2O RHF with HGH at h = 0.25 (64^3 here; the 128^3 case is the benchmark) -> mixed against
+water:    H2O RHF with HGH at h = 0.25 (64^3 here; the 128^3 case is the benchmark) -> mixed against
           FP64 at convergence, FP64 against the oracle on the first iteration.
-config 4: Hellmann-Feynman forces of the mixed path against FP64 central differences (1e-3 bohr) and
+forces:   Hellmann-Feynman forces of the mixed path against FP64 central differences (1e-3 bohr) and
           a few Adam steps that lower the energy.
 """
 import math
@@ -31,7 +31,7 @@ def dev(x, dtype=torch.float64):
     return torch.as_tensor(np.ascontiguousarray(x)).to("cuda", dtype)
 
 
-def test_config1_hydrogen_lanczos():
+def test_hydrogen64_lanczos():
     from gato_gb300.grid import Grid3D
     from gato_gb300.hamiltonian import Hamiltonian
     from gato_gb300.potentials import softened_coulomb
@@ -60,7 +60,7 @@ def _helium_inputs(N=96, L=16.0, seed=3):
 HE_KW = dict(mixing=0.5, order=4, epsilon=0.1)
 
 
-def test_config2_helium_first_iteration_vs_oracle():
+def test_helium_first_iteration_vs_oracle():
     from gato_gb300.grid import Grid3D
     from gato_gb300.potentials import softened_coulomb
     from gato_gb300.scf import scf_rhf
@@ -90,12 +90,12 @@ def _helium_mixed_vs_fp64(N, L):
     return full
 
 
-def test_config2_helium_mixed_vs_fp64_64():
+def test_helium64_mixed_vs_fp64():
     _helium_mixed_vs_fp64(64, 16.0)
 
 
 @pytest.mark.skipif(not __import__("os").environ.get("GATO_SLOW"), reason="set GATO_SLOW=1: 96^3 FP64 SCF")
-def test_config2_helium_mixed_vs_fp64_96():
+def test_helium96_mixed_vs_fp64():
     _helium_mixed_vs_fp64(96, 16.0)
 
 
@@ -107,7 +107,7 @@ def _water(N, h, seed=11):
     return Nuclei(nuc.positions + jit, nuc.charges)
 
 
-def test_config3_water_scf_mixed_vs_fp64():
+def test_water_scf_mixed_vs_fp64():
     from gato_gb300.grid import Grid3D
     from gato_gb300.physics.water import solve_rhf_at_geometry, water_hgh_elements
     N, h = 64, 0.25
@@ -146,7 +146,7 @@ def _fock_rayleigh(orbitals, nuc, el, g, dtype):
     return ((f64 * Ff).flatten(1).sum(1) / (f64 * f64).flatten(1).sum(1)).cpu().numpy()
 
 
-def test_config3_water_first_iteration_vs_oracle():
+def test_water_first_iteration_vs_oracle():
     from gato_gb300.grid import Grid3D
     from gato_gb300.physics.water import solve_rhf_at_geometry, water_hgh_elements
     N, h = 48, 0.3
@@ -159,7 +159,7 @@ def test_config3_water_first_iteration_vs_oracle():
     assert np.max(np.abs(got.orbital_energies.cpu().numpy() - ref.orbital_energies)) < 1e-10
 
 
-def test_config4_forces_against_fd_and_adam():
+def test_water_forces_against_fd_and_adam():
     from gato_gb300.grid import Grid3D
     from gato_gb300.physics.water import (bo_energy, hellmann_feynman_force, optimize_water_geometry,
                                           solve_rhf_at_geometry, water_hgh_elements)
