@@ -934,18 +934,19 @@ bool bulk_ok(const T* Vb, int64_t n) {
   return ((uint64_t)n * sizeof(T)) % 16 == 0 && ((uintptr_t)Vb % 16) == 0;
 }
 
-template <typename K>
-int bulk_smem_attr(K kern, size_t bytes) {
-  // opt in to the carve-out once per device and size (the kernels take up to ~64 KB)
+// Opt in to the carve-out once per device and kernel (the kernels take up to
+// ~64 KB). The flag is a static of this template's instantiation for the
+// kernel itself: kernels of one signature must not share it.
+template <auto Kern>
+int bulk_smem_attr() {
   static std::atomic<unsigned> done{0};
   int dev = 0;
   GATO_CUDA_TRY(cudaGetDevice(&dev));
   const unsigned bit = 1u << (dev & 31);
   if (!(done.load() & bit)) {
-    GATO_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+    GATO_CUDA_TRY(cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
     done.fetch_or(bit);
   }
-  (void)bytes;
   return GATO_OK;
 }
 
@@ -959,12 +960,12 @@ int gemv_t_bulk(const T* V, int64_t ld, int nk, const T* W, const Pre<T>& pre, i
   int64_t per = (n + nblk - 1) / nblk;
   per = (per + 31) / 32 * 32;
   if ((per + BulkGeom<T>::CH - 1) / BulkGeom<T>::CH <= kVmChunks) {
-    GATO_TRY(bulk_smem_attr(k_gemv_t_vm<T>, sm));
+    GATO_TRY(bulk_smem_attr<k_gemv_t_vm<T>>());
     k_gemv_t_vm<T><<<nblk, kBulkThreads, sm, s>>>(V, ld, nk, W, pre, n, part, device_error_word());
     GATO_LAUNCH_TRY();
     return GATO_OK;
   }
-  GATO_TRY(bulk_smem_attr(k_gemv_t_bulk<T>, sm));
+  GATO_TRY(bulk_smem_attr<k_gemv_t_bulk<T>>());
   k_gemv_t_bulk<T><<<nblk, kBulkThreads, sm, s>>>(V, ld, nk, W, pre, n, part, device_error_word());
   GATO_LAUNCH_TRY();
   return GATO_OK;
@@ -975,7 +976,7 @@ int gemv_n_bulk(const T* V, int64_t ld, int nk, T* W, const Pre<T>& pre, const d
                 double* part, cudaStream_t s) {
   const size_t sm = (size_t)kBulkStages * BulkGeom<T>::CH * sizeof(T) + 2 * kBulkStages * sizeof(uint64_t) +
                     (size_t)nk * sizeof(double);
-  GATO_TRY(bulk_smem_attr(k_gemv_n_bulk<T>, sm));
+  GATO_TRY(bulk_smem_attr<k_gemv_n_bulk<T>>());
   k_gemv_n_bulk<T><<<nblk, kBulkThreads, sm, s>>>(V, ld, nk, W, pre, c, n, part, device_error_word());
   GATO_LAUNCH_TRY();
   return GATO_OK;

@@ -450,6 +450,28 @@ def test_lanczos_ho_ladder_kat():                        # reference test_lanczo
         assert abs(got - want) < 5e-3
 
 
+def test_lanczos_both_sweep_layouts_in_one_process():
+    """Small grids take the vector-major coefficient sweep, 160^3 the chunk-major one; both run in one
+    process (each kernel opts in to its own shared-memory carve-out). Only the first Lanczos coefficients
+    are well conditioned on a fine grid (in the oracle, FP32-sized noise on the start vector moves alpha_2
+    at 160^3 by 6e-3 relative, and a 1e-10 change moves the m = 60 Ritz value by 1e-3), so FP32 and FP64
+    are compared on alpha_0, alpha_1 and beta_0."""
+    from gato_gb300.grid import Grid3D
+    from gato_gb300.hamiltonian import Hamiltonian
+    from gato_gb300.potentials import softened_coulomb
+    from gato_gb300.solvers.lanczos import lanczos
+    for N, L in ((32, 12.0), (160, 12.0)):
+        g = Grid3D(N, L)
+        X, Y, Z = g.coords()
+        coef = {}
+        for dt in (torch.float32, torch.float64):
+            H = Hamiltonian(g, softened_coulomb(g, 1.0, 0.5, dtype=dt), order=4)
+            psi0 = torch.exp(-(X * X + Y * Y + Z * Z) / 2).to(dt)
+            res = lanczos(H, psi0, 12, 1)
+            coef[dt] = np.concatenate([host(res.alphas)[:2], host(res.betas)[:1]])
+        assert np.max(np.abs(coef[torch.float32] - coef[torch.float64])) < 1e-5 * np.max(np.abs(coef[torch.float64]))
+
+
 def test_scf_history_golden():
     """Plain FP64 SCF reproduces the oracle iteration by iteration."""
     from gato_gb300.grid import Grid3D
