@@ -238,12 +238,20 @@ __device__ __forceinline__ int64_t box_global(const int* bx, int64_t t, int N) {
   return ((int64_t)x * N + y) * N + z;
 }
 
-// grid (nq, kChunks, nb): partials[(b*nq + q)*kChunks + chunk] = sum p*psi
+// grid (nq, kChunks, nb): partials[(b*nq + q)*kChunks + chunk] = sum p*psi.
+// The last block to finish (a ticket counter, the threadfence-reduction
+// pattern: no block waits for another) then reduces the partials of every
+// (b, q) in the k_finalize_sums order, ov = dV * sum, and forms
+// coef[b][q] = sum_j h_ij ov[b][block + j]; it resets the ticket for the next
+// launch. One launch instead of overlap + finalize + coefficient launches.
 template <typename T>
 __global__ void k_nl_overlap(const T* __restrict__ psi, const T* __restrict__ vals, const int* q_atom,
-                             const int64_t* q_off, const int* boxes, int N, double* part) {
+                             const int64_t* q_off, const int* boxes, int N, double* part, double dV,
+                             double* ov, double* coef, const int* q_block, const int* q_n, const int* q_i,
+                             const double* q_h, unsigned* ticket) {
   __shared__ double sh[32];
-  const int q = blockIdx.x, chunk = blockIdx.y, b = blockIdx.z, nq = gridDim.x;
+  __shared__ bool last;
+  const int q = blockIdx.x, chunk = blockIdx.y, b = blockIdx.z, nq = gridDim.x, nb = gridDim.z;
   const int a = q_atom[q];
   const int* bx = boxes + 6 * a;
   const int64_t npts = (int64_t)bx[3] * bx[4] * bx[5];
@@ -254,33 +262,56 @@ __global__ void k_nl_overlap(const T* __restrict__ psi, const T* __restrict__ va
        t += (int64_t)gridDim.y * blockDim.x)
     acc.add_prod(pv[t], ps[box_global(bx, t, N)]);
   const double v = block_sum(acc.value(), sh);
-  if (threadIdx.x == 0) part[((int64_t)b * nq + q) * gridDim.y + chunk] = v;
-}
-
-// coef[b][q] = sum_j h_ij ov[b][block + j]   (one thread per (b, q))
-__global__ void k_nl_coef(const double* ov, double* coef, const int* q_block, const int* q_n,
-                          const int* q_i, const double* q_h, int nq, int nb) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nq * nb) return;
-  const int b = t / nq, q = t % nq;
-  const int blk = q_block[q], n = q_n[q], i = q_i[q];
-  double c = 0.0;
-  for (int j = 0; j < n; ++j) c += q_h[9 * q + 3 * i + j] * ov[b * nq + blk + j];
-  coef[t] = c;
+  if (threadIdx.x == 0) {
+    part[((int64_t)b * nq + q) * gridDim.y + chunk] = v;
+    __threadfence();   // the partial is visible before the ticket counts this block
+    const unsigned total = gridDim.x * gridDim.y * gridDim.z;
+    last = atomicAdd(ticket, 1u) == total - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const int nqb = nq * nb, nch = gridDim.y;
+  for (int j = 0; j < nqb; ++j) {
+    double sum = 0.0;
+    for (int i = threadIdx.x; i < nch; i += blockDim.x) sum += __ldcg(part + (int64_t)j * nch + i);
+    sum = block_sum(sum, sh);
+    if (threadIdx.x == 0) ov[j] = sum * dV;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nqb; t += blockDim.x) {
+    const int bb = t / nq, qq = t % nq;
+    const int blk = q_block[qq], n = q_n[qq], i = q_i[qq];
+    double c = 0.0;
+    for (int j = 0; j < n; ++j) c += q_h[9 * qq + 3 * i + j] * ov[bb * nq + blk + j];
+    coef[t] = c;
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
 }
 
 // out[b][box pt] += sum_{q in atom} coef[b][q] * p_q(pt)
+// The atom's coefficients (rounded once to the field type) and value offsets
+// are staged in shared memory, so no element converts from FP64.
+constexpr int kNlAddMaxQ = 64;   // projectors of one atom (HGH: at most 2 (2l+1) per l <= 2)
+
 template <typename T>
 __global__ void k_nl_add(T* out, const T* __restrict__ vals, const double* coef, const int64_t* q_off,
                          const int* boxes, int atom, int q0, int nqa, int nq, int N) {
+  __shared__ T cf[kNlAddMaxQ];
+  __shared__ int64_t off[kNlAddMaxQ];
   const int* bx = boxes + 6 * atom;
   const int64_t npts = (int64_t)bx[3] * bx[4] * bx[5];
   const int b = blockIdx.y;
+  for (int k = threadIdx.x; k < nqa; k += blockDim.x) {
+    cf[k] = (T)coef[b * nq + q0 + k];
+    off[k] = q_off[q0 + k];
+  }
+  __syncthreads();
   T* o = out + (int64_t)b * N * N * N;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < npts;
        t += (int64_t)gridDim.x * blockDim.x) {
     T s = (T)0;
-    for (int k = 0; k < nqa; ++k) s += (T)coef[b * nq + q0 + k] * vals[q_off[q0 + k] + t];
+    for (int k = 0; k < nqa; ++k) s += cf[k] * vals[off[k] + t];
     o[box_global(bx, t, N)] += s;
   }
 }
@@ -369,15 +400,12 @@ int nl_overlaps(Nonlocal& nl, const void* psi, int nb, cudaStream_t s) {
   dim3 g(nl.nq, Nonlocal::kChunks, nb);
   if (nl.dtype == GATO_F64)
     k_nl_overlap<double><<<g, 256, 0, s>>>((const double*)psi, (const double*)nl.vals, nl.d_q_atom,
-                                           nl.d_q_off, nl.d_box, nl.N, nl.part);
+                                           nl.d_q_off, nl.d_box, nl.N, nl.part, nl.dV, nl.ov, nl.coef,
+                                           nl.d_q_block, nl.d_q_n, nl.d_q_i, nl.d_q_h, nl.ticket);
   else
     k_nl_overlap<float><<<g, 256, 0, s>>>((const float*)psi, (const float*)nl.vals, nl.d_q_atom,
-                                          nl.d_q_off, nl.d_box, nl.N, nl.part);
-  GATO_LAUNCH_TRY();
-  GATO_TRY(finalize_sums(nl.part, nl.nq * nb, Nonlocal::kChunks, nl.dV, nl.ov, s));
-  const int nt = nl.nq * nb;
-  k_nl_coef<<<(nt + 127) / 128, 128, 0, s>>>(nl.ov, nl.coef, nl.d_q_block, nl.d_q_n, nl.d_q_i,
-                                             nl.d_q_h, nl.nq, nb);
+                                          nl.d_q_off, nl.d_box, nl.N, nl.part, nl.dV, nl.ov, nl.coef,
+                                          nl.d_q_block, nl.d_q_n, nl.d_q_i, nl.d_q_h, nl.ticket);
   GATO_LAUNCH_TRY();
   return GATO_OK;
 }
@@ -390,6 +418,7 @@ int nonlocal_apply(Nonlocal& nl, const void* psi, void* out, int nb, cudaStream_
   GATO_TRY(nl_overlaps(nl, psi, nb, s));
   for (int a = 0; a < nl.K; ++a) {
     if (nl.atom_nq[a] == 0) continue;
+    if (nl.atom_nq[a] > kNlAddMaxQ) return fail(GATO_EUNSUPPORTED, "nonlocal: more than %d projectors on one atom", kNlAddMaxQ);
     const int64_t npts = nl.box[a].npts;
     dim3 g(grid_for(npts, 256, 152 * 4), nb);
     if (nl.dtype == GATO_F64)
@@ -617,6 +646,9 @@ extern "C" int gato_nonlocal_create(int dtype, int N, double L, int K, const dou
   alloc((void**)&nl.coef, nvq * sizeof(double));
   alloc((void**)&nl.dov, nvq * 3 * sizeof(double));
   alloc((void**)&nl.part, nvq * 3 * Nonlocal::kChunks * sizeof(double));
+  alloc((void**)&nl.ticket, sizeof(unsigned));
+  if (nl.ticket && cudaMemset(nl.ticket, 0, sizeof(unsigned)) != cudaSuccess)
+    st = fail(GATO_ECUDA, "nonlocal: ticket reset failed");
   up(nl.d_q_atom, q_atom.data(), nq * sizeof(int));
   up(nl.d_q_off, q_off.data(), nq * sizeof(int64_t));
   up(nl.d_q_block, q_block.data(), nq * sizeof(int));
@@ -648,7 +680,7 @@ extern "C" int gato_nonlocal_destroy(gato_nonlocal_t w) {
   if (!w) return GATO_OK;
   Nonlocal& nl = w->n;
   free_after_pending({nl.vals, nl.d_q_atom, nl.d_q_off, nl.d_q_block, nl.d_q_n, nl.d_q_i, nl.d_q_h, nl.d_box,
-                      nl.ov, nl.coef, nl.dov, nl.part});
+                      nl.ov, nl.coef, nl.dov, nl.part, nl.ticket});
   delete w;
   return GATO_OK;
 }

@@ -49,6 +49,7 @@ struct Nonlocal {
   double* coef = nullptr;           // [vec][q]
   double* part = nullptr;           // partials
   double* dov = nullptr;            // [vec][q][3]
+  unsigned* ticket = nullptr;       // blocks done in the running overlap launch (0 between launches)
   static constexpr int kMaxVec = 16;
   static constexpr int kChunks = 32;  // partial sums per projector box
 };
