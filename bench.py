@@ -190,26 +190,19 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def e2e_pipelined(st, g, host_in, steps):
+def e2e_pipelined(st, st_b, host_in, steps):
     """Seconds for `steps` block applies through the public API from pinned host memory, pipelined.
 
-    Two operators (one per device orbital buffer) alternate: step k's host-to-device copy runs on
-    an upload stream and step k's result comes back on a download stream, so the copies of one step
-    overlap the compute of its neighbours. Each step still copies its own inputs in and its whole
-    result out; the window runs from the first upload to the last download."""
+    Two operators (each with its own orbital buffer, Poisson plan and projector scratch) alternate,
+    each computing on its own stream: step k's host-to-device copy runs on an upload stream, step k's
+    result comes back on a download stream, and step k's kernels may overlap step k-1's. Each step
+    still copies its own inputs in and its whole result out; the window runs from the first upload
+    to the last download."""
     import torch
-    from gato_gb300.scf import Operator
     comp = torch.cuda.current_stream()
+    comps = [comp, torch.cuda.Stream()]
     up, down = torch.cuda.Stream(), torch.cuda.Stream()
-    ops, bufs, outs = [st["op"]], [st["fields"]], [st["out"]]
-    op2 = Operator(g, torch.float32, 4, "dirichlet")
-    op2.set_potential(st["op"]._keep["V"])
-    op2.set_nonlocal(st["op"]._keep["nl"])
-    op2.tune(st["op"].block_epilogue)
-    bufs.append(torch.empty_like(st["fields"]))
-    op2.set_exchange(st["plan"], bufs[1])
-    ops.append(op2)
-    outs.append(torch.empty_like(st["out"]))
+    ops, bufs, outs = [st["op"], st_b["op"]], [st["fields"], st_b["fields"]], [st["out"], st_b["out"]]
     hosts = [torch.empty_like(host_in).pin_memory() for _ in range(2)]
     ev = lambda: torch.cuda.Event()   # noqa: E731
     try:   # each operator's block apply as a graph replay, as in the headline
@@ -223,9 +216,11 @@ def e2e_pipelined(st, g, host_in, steps):
         t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0.record(comp)
         up.wait_event(t0)
+        comps[1].wait_event(t0)
         loaded = []
         for k in range(n):
             b = k % 2
+            cs = comps[b]
             with torch.cuda.stream(up):
                 if done[b] is not None:
                     up.wait_event(done[b])
@@ -233,17 +228,19 @@ def e2e_pipelined(st, g, host_in, steps):
                 e = ev()
                 e.record(up)
                 loaded.append(e)
-            comp.wait_event(loaded[k])
+            cs.wait_event(loaded[k])
             if k >= 2:
-                comp.wait_event(dl[b])   # the buffer's previous result is home
-            steps_fn[b]()
+                cs.wait_event(dl[b])   # the buffer's previous result is home
+            with torch.cuda.stream(cs):
+                steps_fn[b]()
             done[b] = ev()
-            done[b].record(comp)
+            done[b].record(cs)
             with torch.cuda.stream(down):
                 down.wait_event(done[b])
                 hosts[b].copy_(outs[b], non_blocking=True)
                 dl[b] = ev()
                 dl[b].record(down)
+        comp.wait_stream(comps[1])
         comp.wait_stream(down)
         t1.record(comp)
         t1.synchronize()
@@ -359,6 +356,21 @@ def run_gato(args):
                        "block_epilogue": epi["epilogue"],
                        "epilogue_ms": {str(c["epilogue"]): round(c["ms"], 4) for c in epi["candidates"]}}
 
+    # a second FP32 operator over its own orbital buffer, Poisson plan and projector scratch, so that
+    # two block applies can be in flight on two streams (the plan's spectral buffers and the
+    # projectors' overlap sums are per object, so one object serves one stream at a time)
+    from gato_gb300.autotune import set_plan
+    from gato_gb300.solvers.poisson import PoissonPlan
+    plan_b = PoissonPlan(N, h, eps, torch.float32, pair_fields(N_OCC))
+    set_plan(plan_b, tuned["mixed"]["group"], tuned["mixed"]["engine"])
+    op_b = Operator(g, torch.float32, 4, "dirichlet")
+    op_b.set_potential(s32["op"]._keep["V"])
+    op_b.set_nonlocal(nonlocal_for(nuc, el, g, torch.float32))
+    op_b.tune(s32["op"].block_epilogue)
+    fields_b = s32["fields"].clone()
+    op_b.set_exchange(plan_b, fields_b)
+    s32b = dict(op=op_b, fields=fields_b, out=torch.empty_like(s32["out"]))
+
     def timed(fn, steps, warmup):
         for _ in range(warmup):
             fn()
@@ -401,6 +413,32 @@ def run_gato(args):
             times = timed(lambda: op32.apply_block(s32["out"]), args.steps, 0)
             launches = (_lib.launch_count() - l0) // max(args.steps, 1) * args.steps
     value, t_max = job_rate(sum(times), args.steps, world, dist, dev)
+
+    # two steps in flight: the second operator's step replays on its own stream beside the first's
+    # (no L2 flush between steps here: each step streams ~2.4 GB, far more than L2 holds)
+    two_streams = None
+    if graph is not None:
+        graph_b = s32b["op"].block_graph(s32b["out"])
+        sb = torch.cuda.Stream()
+
+        def two(n):
+            cur = torch.cuda.current_stream()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(cur)
+            sb.wait_stream(cur)
+            for _ in range(n // 2):
+                graph.replay()
+                with torch.cuda.stream(sb):
+                    graph_b.replay()
+            cur.wait_stream(sb)
+            e1.record(cur)
+            e1.synchronize()
+            return e0.elapsed_time(e1) * 1e-3
+        two(6)
+        n2 = 2 * max(3, args.steps // 2)
+        two_streams = {"value": n2 / two(n2), "steps": n2,
+                       "mode": "two operators, each step a graph replay on its own stream"}
+        del graph_b
 
     # ---- plain FP64 and matvec rates ----------------------------------------------
     k64 = max(2, args.steps // 4)
@@ -478,7 +516,7 @@ def run_gato(args):
         host_out.copy_(s32["out"], non_blocking=True)
     te = timed(e2e_step, args.steps, 2)
     e2e_serial = world * args.steps / sum(te)
-    e2e_val, _ = job_rate(e2e_pipelined(s32, g, host_in, args.steps), args.steps, world, dist, dev)
+    e2e_val, _ = job_rate(e2e_pipelined(s32, s32b, host_in, args.steps), args.steps, world, dist, dev)
 
     if rank != 0:
         if world > 1:
@@ -503,12 +541,15 @@ def run_gato(args):
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": host_in.numel() * 4,
                 "d2h_bytes_per_step": host_out.numel() * 4,
                 "mode": "two-deep pipeline: step k+1's orbitals copy in and step k-1's result copies out "
-                        "on their own streams while step k computes; every step copies its own inputs "
-                        "and result (no L2 flush: the step streams ~1 GB of spectral buffers)",
+                        "on their own streams while step k computes; consecutive steps alternate between "
+                        "two operators (own plan and projector scratch) computing on two streams, so "
+                        "their kernels may overlap; every step copies its own inputs and result (no L2 "
+                        "flush: the step streams ~2.4 GB of spectral buffers)",
                 "serial_value": e2e_serial},
         "gpu_launches": int(launches),
         "cuda_graph": ({"used": True, "kernels_per_step": per_step,
-                        "direct_launch_value": world * args.steps / sum(direct)} if graph is not None
+                        "direct_launch_value": world * args.steps / sum(direct),
+                        "two_streams": two_streams} if graph is not None
                        else {"used": False, "error": graph_error,
                              "direct_launch_value": world * args.steps / sum(direct)}),
         "roofline": {"kernel": "k_cols<float2, FMI> (x FFT, kernel multiply, inverse x FFT)", "bound": "hbm",
