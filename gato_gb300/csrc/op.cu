@@ -73,6 +73,36 @@ static void block_pairs(PassArgs& a, const gato_operator& op, void* out, bool en
   }
   a.nout = energy ? 0 : n;
   int part = 0;
+  const int nd = n, no = n * (n - 1) / 2;
+  const int f_mixed = (1 + nd + no + 1) / 2, f_split = 1 + (nd + 1) / 2 + (no + 1) / 2;
+  if (energy && op.pp && poisson_j_supported(op.pp->p) && f_split < 2 * f_mixed) {
+    // The spectral energy pass (half the work of a field's full solve) sums
+    // both parts of a field with one weight: the density rides alone, the
+    // diagonal pairs (weight -1) and the off-diagonal pairs (weight -2) fill
+    // fields of their own.
+    a.in[n] = op.rho;
+    PartDesc& d = a.f[0].p[0];
+    d.a = (int8_t)n;
+    d.ew = 0.5;
+    d.eslot = 0;
+    int nf = 1;
+    for (int w = 0; w < 2; ++w) {
+      part = 0;
+      for (int i = 0; i < n; ++i)
+        for (int j = i; j < n; ++j) {
+          if ((i == j) != (w == 0)) continue;
+          PartDesc& e = a.f[nf + part / 2].p[part % 2];
+          e.a = (int8_t)i;
+          e.b = (int8_t)j;
+          e.ew = i == j ? -1.0 : -2.0;   // E_x = -sum_ij <phi_i phi_j | J[phi_i phi_j]>
+          e.eslot = 1;
+          ++part;
+        }
+      nf += (part + 1) / 2;
+    }
+    a.nf = nf;
+    return;
+  }
   if (energy) {
     // the density rides first: E_H = 1/2 dV sum rho J[rho]
     a.in[n] = op.rho;

@@ -305,7 +305,27 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
   const int nblk_i = (int)((nrows + Linv - 1) / Linv);
   const int group = pl.group > 0 ? std::min(pl.group, pl.max_fields) : pl.max_fields;
   const int ngroups = (args.nf + group - 1) / group;
-  if (epi == EPI_ENERGY && (int64_t)ngroups * 2 * nblk_i > pl.npart_cap)
+  // Energies on the register engine take the spectral (Parseval) pass when
+  // both parts of every field carry one weight and one slot: x forward and the
+  // kernel-weighted power, no x, y or z inverse.
+  bool fe = epi == EPI_ENERGY && Lf > 0;
+  const int64_t fe_nb = fe ? (int64_t)M * ((M + Lf - 1) / Lf) : 0;   // x-pass CTAs per field
+  FeArgs fa;
+  if (fe) {
+    for (int f = 0; f < args.nf && fe; ++f) {
+      const PartDesc& p0 = args.f[f].p[0];
+      const PartDesc& p1 = args.f[f].p[1];
+      const PartDesc& pw = p0.a >= 0 ? p0 : p1;
+      fe = (p0.a < 0 || p1.a < 0 || (p0.ew == p1.ew && p0.eslot == p1.eslot)) && pw.eslot >= 0 &&
+           pw.eslot <= 1;
+      fa.w[f] = pw.a >= 0 ? pw.ew : 0.0;
+      fa.slot[f] = pw.eslot;
+    }
+    fe = fe && 2 * args.nf * fe_nb <= pl.npart_cap;
+    fa.partials = pl.partials;
+    fa.slot_stride = args.nf * fe_nb;
+  }
+  if (epi == EPI_ENERGY && !fe && (int64_t)ngroups * 2 * nblk_i > pl.npart_cap)
     return fail(GATO_EUNSUPPORTED, "poisson: energy partials exceed plan capacity");
   if (Lf == 0) {
     GATO_TRY(set_smem(k_rows_fwd<T>, sm_r));
@@ -326,6 +346,11 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
       // engine 0: multi-field z forward from two fields, 2: never, 3: from three
       GATO_TRY(fast::rows_fwd<T>(M, args, f0, nfg, S1, tw2, pl.engine == 2 ? 0 : (pl.engine == 3 ? 1 : 2), s));
       GATO_TRY(fast::cols<T>(M, COL_FWD, S1, S2, gy, N, nfg, tw2, nullptr, pl.H, s));
+      if (fe) {
+        fa.f0 = f0;
+        GATO_TRY(fast::cols_fe<T>(M, S2, gx, M, nfg, tw2, (const T*)pl.ghat, pl.H, fa, s));
+        continue;
+      }
       GATO_TRY(fast::cols<T>(M, COL_FMI, S2, S2, gx, M, nfg, tw2, (const T*)pl.ghat, pl.H, s));
       GATO_TRY(fast::cols<T>(M, COL_INV, S2, S1, gyi, N, nfg, tw2, nullptr, pl.H, s));
       if (epi == EPI_J)
@@ -356,8 +381,9 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
     GATO_LAUNCH_TRY();
   }
   if (epi == EPI_ENERGY) {
-    // partials laid out [slot][group][block]
-    GATO_TRY(finalize_sums(pl.partials, 2, ngroups * nblk_i, pl.dV, energy_dev, s));
+    // partials laid out [slot][group][row block], or [slot][field][x-pass block]
+    const int64_t nparts = fe ? args.nf * fe_nb : (int64_t)ngroups * nblk_i;
+    GATO_TRY(finalize_sums(pl.partials, 2, (int)nparts, pl.dV, energy_dev, s));
   }
   return GATO_OK;
 }
@@ -450,8 +476,11 @@ static int plan_create(int dtype, int N, double h, double eps, int max_fields, P
   const size_t cs = 2 * ts;
   GATO_CUDA_TRY(cudaMalloc(&pl.S1, (size_t)max_fields * N * N * M * cs));
   GATO_CUDA_TRY(cudaMalloc(&pl.S2, (size_t)max_fields * N * M * M * cs));
-  // energy partials: 2 slots x (groups of a 40-field call) x row blocks (L >= 1)
+  // energy partials: 2 slots x (groups of a 40-field call) x row blocks (L >= 1);
+  // the spectral pass needs 2 slots x fields x x-pass CTAs (room for 2 max_fields)
   pl.npart_cap = 2 * ((kMaxFields + max_fields - 1) / max_fields) * N * N;
+  const int Lc = dtype == GATO_F32 ? fast::rows_L<float>(M) : fast::rows_L<double>(M);
+  if (Lc > 0) pl.npart_cap = std::max(pl.npart_cap, 2 * 2 * max_fields * M * ((M + Lc - 1) / Lc));
   GATO_CUDA_TRY(cudaMalloc(&pl.partials, (size_t)pl.npart_cap * sizeof(double)));
   return GATO_OK;
 }

@@ -73,6 +73,18 @@ __device__ __forceinline__ T dens(const PartDesc& d, const void* const* in, int6
   return v;
 }
 
+// Weights of the spectral (Parseval) energy pass: field f of a call adds
+// w[f] * sum_k ghat(k) |F_f(k)|^2 to energy slot slot[f]. Partials are laid
+// out [slot][field][y block][x block] of the x-pass grid, slot_stride entries
+// per slot.
+struct FeArgs {
+  double* partials = nullptr;
+  int64_t slot_stride = 0;
+  int f0 = 0;                  // first field of this launch within the call
+  double w[kMaxFields] = {};
+  int8_t slot[kMaxFields] = {};
+};
+
 // Register-resident two-pass kernels for the common sizes M = 2N (see
 // fft2.cuh); each returns kNotHandled when M has no instantiation.
 namespace fast {
@@ -83,6 +95,12 @@ template <typename T>
 int cols(int M, int mode, const typename Cplx<T>::type* in, typename Cplx<T>::type* out,
          const ColGeom& g, int outer, int nf, const typename Cplx<T>::type* tw, const T* ghat,
          int H, cudaStream_t s);
+// x forward of the y-transformed fields and the kernel-weighted spectral power
+// per CTA (the energy epilogue without the inverse passes).
+template <typename T>
+int cols_fe(int M, const typename Cplx<T>::type* in, const ColGeom& g, int outer, int nf,
+            const typename Cplx<T>::type* tw, const T* ghat, int H, const FeArgs& fa,
+            cudaStream_t s);
 template <typename T>
 int rows_fwd(int M, const PassArgs& a, int f0, int nfg, typename Cplx<T>::type* S1,
              const typename Cplx<T>::type* tw, int multi, cudaStream_t s);

@@ -115,6 +115,99 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   }
 }
 
+// Block sum of a per-thread accumulator, valid in thread 0 only: float-float
+// through the shuffles for FP32 (the FP64 pipe is used once per CTA), double
+// for FP64. `sh` holds 32 doubles.
+__device__ __forceinline__ double block_sum0(const Acc<float>& a, double* sh) {
+  FF s = a.s;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float hi = __shfl_xor_sync(0xffffffffu, s.hi, o);
+    const float lo = __shfl_xor_sync(0xffffffffu, s.lo, o);
+    ff_add(s, hi);
+    s.lo += lo;
+  }
+  float2* shf = reinterpret_cast<float2*>(sh);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) shf[warp] = make_float2(s.hi, s.lo);
+  __syncthreads();
+  if (threadIdx.x != 0) return 0.0;
+  FF t{0.f, 0.f};
+  for (int w = 0; w < nw; ++w) {
+    ff_add(t, shf[w].x);
+    t.lo += shf[w].y;
+  }
+  return ff_value(t);
+}
+__device__ __forceinline__ double block_sum0(const Acc<double>& a, double* sh) {
+  return block_sum(a.value(), sh);
+}
+
+// Energies without the inverse passes (Parseval). The kernel spectrum is
+// stored as ghat = G^ dV / M^3, so a part's epilogue energy sum_r rho J with
+// J = IDFT(ghat DFT(rho)) (unnormalised) equals sum_k ghat(k) |rho^(k)|^2 over
+// the doubled grid (rho is zero outside the N^3 box). For a field F = a + i b
+// of two real densities, sum_k ghat |F^|^2 is the sum of both parts' values:
+// ghat is real and even, so the cross terms cancel between k and -k. Both
+// parts of a field therefore carry one weight and one slot. Each CTA runs the
+// x forward transform of its lines of the y-transformed field (as the x pass
+// does), sums ghat |X|^2 over its spectrum entries and writes the weighted sum
+// to its field's slot, 0 to the other slot.
+template <typename T, int R1, int R2, int L, bool FULL>
+__global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
+    k_cols_fe(const typename Cplx<T>::type* in, ColGeom g, const typename Cplx<T>::type* tw,
+              const T* ghat, int H, FeArgs fa) {
+  using T2 = typename Cplx<T>::type;
+  constexpr int M = R1 * R2, LP = L + 1;
+  static_assert(R2 % 2 == 0, "the octant fold below splits k2 at R2 / 2");
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ double sh[32];
+  T2* buf = reinterpret_cast<T2*>(smraw);
+  T2* tws = buf + M * LP;
+  const TwPrefetch<T2, R1 * TwRow<T2, R2>::S, L * Shape<R1, R2>::RMAX> twp(tw);
+  const int outer = blockIdx.x, col0 = blockIdx.y * L, f = blockIdx.z;
+  const int t = threadIdx.x;
+  const int line = t % L, q = t / L;
+  const bool live = FULL || line < g.ncols - col0;
+  const T2* src = in + f * g.in_fs + outer * g.in_os + col0 + line;
+  const int64_t ips = g.in_ps;
+  if (q < R2) {
+    const T2* b1 = src + q * ips;
+    fwd_stage1<T2, R1, R2, true>(buf, LP, line, q, [&](int pos) {
+      T2 v;
+      if (live) v = b1[(pos - q) * ips];
+      else v.x = v.y = 0;
+      return v;
+    });
+  }
+  twp.store(tws);
+  __syncthreads();
+  Acc<T> acc;
+  if (q < R1) {
+    T2 X[R2];
+    fwd_stage2<T2, R1, R2>(buf, LP, line, q, tws, X);
+    // kx = q + R1 k2, folded into the kernel-spectrum octant as in the x pass
+    const int ky = outer, kyo = ky <= M - ky ? ky : M - ky;
+    const int kz = col0 + line, kzo = kz <= M - kz ? kz : M - kz;
+    const int64_t HH = (int64_t)H * H, st = (int64_t)R1 * HH;
+    const T* glo = ghat + (int64_t)q * HH + (int64_t)kyo * H + kzo;
+    const T* ghi = ghat + (int64_t)(M - q) * HH + (int64_t)kyo * H + kzo;
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) {
+      const T gv = live ? (k2 < R2 / 2 ? glo[k2 * st] : ghi[-k2 * st]) : (T)0;
+      acc.add_prod(gv, X[k2].x * X[k2].x + X[k2].y * X[k2].y);
+    }
+  }
+  const double s = block_sum0(acc, sh);
+  if (t == 0) {
+    const int fg = fa.f0 + f;
+    const int64_t b = ((int64_t)fg * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    const double v = fa.w[fg] * s;
+    fa.partials[b] = fa.slot[fg] == 0 ? v : 0.0;
+    fa.partials[fa.slot_stride + b] = fa.slot[fg] == 0 ? 0.0 : v;
+  }
+}
+
 // ---- z passes (rows) ---------------------------------------------------------------
 // A CTA owns L consecutive rows (x, y) of the z axis; thread t works on line
 // t / RMAX as item j = t % RMAX: n2 in stages 1 and B, k1 in stages 2 and A
@@ -513,6 +606,20 @@ struct Launch {
     } else {
       GATO_TRY(smem_attr(k_cols<T, R1, R2, L, COL_FMI, FULL>, sm));
       k_cols<T, R1, R2, L, COL_FMI, FULL><<<grid, NT, sm, s>>>(in, out, g, tw, ghat, H);
+    }
+    GATO_LAUNCH_TRY();
+    return GATO_OK;
+  }
+  static int cols_fe(const T2* in, const ColGeom& g, int outer, int nf, const T2* tw, const T* ghat, int H,
+                     const FeArgs& fa, cudaStream_t s) {
+    dim3 grid(outer, (g.ncols + L - 1) / L, nf);
+    const size_t sm = sm_cols();
+    if (g.ncols % L == 0) {
+      GATO_TRY(smem_attr(k_cols_fe<T, R1, R2, L, true>, sm));
+      k_cols_fe<T, R1, R2, L, true><<<grid, NT, sm, s>>>(in, g, tw, ghat, H, fa);
+    } else {
+      GATO_TRY(smem_attr(k_cols_fe<T, R1, R2, L, false>, sm));
+      k_cols_fe<T, R1, R2, L, false><<<grid, NT, sm, s>>>(in, g, tw, ghat, H, fa);
     }
     GATO_LAUNCH_TRY();
     return GATO_OK;

@@ -360,6 +360,43 @@ def test_energy_terms_golden(dtype):
     assert np.max(np.abs(got - GOLD["water_terms"])) < tol, (got, GOLD["water_terms"])
 
 
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_energy_spectral_pass_matches_full_solve(dtype):
+    """The energy pass sums ghat |F^|^2 over the spectrum (Parseval) instead of running the inverse
+    transforms. On the register engine it must agree with the full pair solves of the generic engine
+    for 1, 2 and 4 orbitals (1 orbital keeps the full solve: the split packing would double its
+    fields), on a grid whose x-pass CTAs do not tile the columns evenly (M = 48 with 32 lines per CTA
+    in FP32), and for the Hartree energy alone."""
+    from gato_gb300.autotune import set_plan
+    from gato_gb300.grid import Grid3D
+    from gato_gb300.scf import Operator, pair_fields
+    from gato_gb300.solvers.poisson import PoissonPlan
+    rtol = 1e-11 if dtype == torch.float64 else 2e-6
+    for N, h in ((24, 0.4), (32, 0.3)):
+        og = o.Grid3D(N, N * h)
+        X, Y, Z = og.coords()
+        rng = np.random.default_rng(N)
+        g = Grid3D(N, N * h)
+        for n in (1, 2, 4):
+            orbs = np.stack([np.exp(-rng.uniform(0.3, 0.8) * ((X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2))
+                             * (1 + 0.2 * X * c[1] - 0.1 * Z)
+                             for c in rng.uniform(-1.5, 1.5, (n, 3))])
+            fields = dev(orbs, dtype).contiguous()
+            plan = PoissonPlan(N, h, h / 2, dtype, pair_fields(n))
+            op = Operator(g, dtype, 4, "dirichlet")
+            op.set_potential(torch.zeros(g.shape, dtype=dtype, device="cuda"))
+            op.set_exchange(plan, fields)
+            rho = (2 * (fields * fields).sum(0)).contiguous()
+            terms, eh = {}, {}
+            for engine in (0, 1):
+                set_plan(plan, plan.max_fields, engine)
+                terms[engine] = op.energy_terms(None).cpu().numpy()
+                eh[engine] = float(plan.energy(rho))
+            np.testing.assert_allclose(terms[0][3:], terms[1][3:], rtol=rtol, atol=0)
+            assert abs(eh[0] - eh[1]) <= rtol * abs(eh[1])
+            assert abs(eh[0] - terms[0][3]) <= 4 * rtol * abs(eh[0])
+
+
 def test_scf_identities_on_gpu():                       # reference test_scf.py:44-94
     from gato_gb300.grid import Grid3D
     from gato_gb300.hamiltonian import Hamiltonian
