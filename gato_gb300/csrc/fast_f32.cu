@@ -43,16 +43,6 @@ int cols<T>(int M, int mode, const T2* in, T2* out, const ColGeom& g, int outer,
 }
 
 template <>
-int cols_fe<T>(int M, const T2* in, const ColGeom& g, int outer, int nf, const T2* tw, const T* ghat, int H,
-               const FeArgs& fa, cudaStream_t s) {
-#define X(MM, A, B, L32, L64) \
-  case MM: return Launch<T, A, B, kF32 ? L32 : L64>::cols_fe(in, g, outer, nf, tw, ghat, H, fa, s);
-  switch (M) { GATO_FAST_SHAPES(X) }
-#undef X
-  return kNotHandled;
-}
-
-template <>
 int rows_fwd<T>(int M, const PassArgs& a, int f0, int nfg, T2* S1, const T2* tw, int multi, cudaStream_t s) {
 #define X(MM, A, B, L32, L64) \
   case MM: return Launch<T, A, B, kF32 ? L32 : L64>::rows_fwd(a, f0, nfg, S1, tw, multi, s);

@@ -12,7 +12,8 @@
 // energy     : kinetic via the stencil's fused <phi, T phi> reduction (no
 //              store), V_ext and V_nl by reductions, E_H and E_x from one
 //              batched pair-solve pass in energy mode (rho with weight 1/2,
-//              pairs with -1 (i = j) or -2 (i < j)).
+//              pairs with -1 (i = j) or -2 (i < j)); FP64 plans stop that pass
+//              at the x-forward spectrum (Parseval).
 #include "op.cuh"
 #include "stencil.cuh"
 
@@ -75,7 +76,7 @@ static void block_pairs(PassArgs& a, const gato_operator& op, void* out, bool en
   int part = 0;
   const int nd = n, no = n * (n - 1) / 2;
   const int f_mixed = (1 + nd + no + 1) / 2, f_split = 1 + (nd + 1) / 2 + (no + 1) / 2;
-  if (energy && op.pp && poisson_j_supported(op.pp->p) && f_split < 2 * f_mixed) {
+  if (energy && op.pp && poisson_fe_supported(op.pp->p) && f_split < 2 * f_mixed) {
     // The spectral energy pass (half the work of a field's full solve) sums
     // both parts of a field with one weight: the density rides alone, the
     // diagonal pairs (weight -1) and the off-diagonal pairs (weight -2) fill

@@ -305,10 +305,10 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
   const int nblk_i = (int)((nrows + Linv - 1) / Linv);
   const int group = pl.group > 0 ? std::min(pl.group, pl.max_fields) : pl.max_fields;
   const int ngroups = (args.nf + group - 1) / group;
-  // Energies on the register engine take the spectral (Parseval) pass when
-  // both parts of every field carry one weight and one slot: x forward and the
-  // kernel-weighted power, no x, y or z inverse.
-  bool fe = epi == EPI_ENERGY && Lf > 0;
+  // FP64 energies on the register engine take the spectral (Parseval) pass
+  // when both parts of every field carry one weight and one slot: x forward
+  // and the kernel-weighted power, no x, y or z inverse.
+  bool fe = epi == EPI_ENERGY && poisson_fe_supported(pl);
   const int64_t fe_nb = fe ? (int64_t)M * ((M + Lf - 1) / Lf) : 0;   // x-pass CTAs per field
   FeArgs fa;
   if (fe) {
@@ -346,10 +346,12 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
       // engine 0: multi-field z forward from two fields, 2: never, 3: from three
       GATO_TRY(fast::rows_fwd<T>(M, args, f0, nfg, S1, tw2, pl.engine == 2 ? 0 : (pl.engine == 3 ? 1 : 2), s));
       GATO_TRY(fast::cols<T>(M, COL_FWD, S1, S2, gy, N, nfg, tw2, nullptr, pl.H, s));
-      if (fe) {
-        fa.f0 = f0;
-        GATO_TRY(fast::cols_fe<T>(M, S2, gx, M, nfg, tw2, (const T*)pl.ghat, pl.H, fa, s));
-        continue;
+      if constexpr (sizeof(T) == 8) {
+        if (fe) {
+          fa.f0 = f0;
+          GATO_TRY(fast::cols_fe<T>(M, S2, gx, M, nfg, tw2, (const T*)pl.ghat, pl.H, fa, s));
+          continue;
+        }
       }
       GATO_TRY(fast::cols<T>(M, COL_FMI, S2, S2, gx, M, nfg, tw2, (const T*)pl.ghat, pl.H, s));
       GATO_TRY(fast::cols<T>(M, COL_INV, S2, S1, gyi, N, nfg, tw2, nullptr, pl.H, s));
@@ -477,9 +479,9 @@ static int plan_create(int dtype, int N, double h, double eps, int max_fields, P
   GATO_CUDA_TRY(cudaMalloc(&pl.S1, (size_t)max_fields * N * N * M * cs));
   GATO_CUDA_TRY(cudaMalloc(&pl.S2, (size_t)max_fields * N * M * M * cs));
   // energy partials: 2 slots x (groups of a 40-field call) x row blocks (L >= 1);
-  // the spectral pass needs 2 slots x fields x x-pass CTAs (room for 2 max_fields)
+  // the FP64 spectral pass needs 2 slots x fields x x-pass CTAs (room for 2 max_fields)
   pl.npart_cap = 2 * ((kMaxFields + max_fields - 1) / max_fields) * N * N;
-  const int Lc = dtype == GATO_F32 ? fast::rows_L<float>(M) : fast::rows_L<double>(M);
+  const int Lc = dtype == GATO_F64 ? fast::rows_L<double>(M) : 0;
   if (Lc > 0) pl.npart_cap = std::max(pl.npart_cap, 2 * 2 * max_fields * M * ((M + Lc - 1) / Lc));
   GATO_CUDA_TRY(cudaMalloc(&pl.partials, (size_t)pl.npart_cap * sizeof(double)));
   return GATO_OK;
@@ -635,6 +637,10 @@ namespace gato {
 bool poisson_j_supported(const PoissonPlan& pl) {
   if (pl.engine == 1) return false;
   return (pl.dtype == GATO_F64 ? fast::rows_L<double>(pl.M) : fast::rows_L<float>(pl.M)) > 0;
+}
+
+bool poisson_fe_supported(const PoissonPlan& pl) {
+  return pl.dtype == GATO_F64 && poisson_j_supported(pl);
 }
 
 namespace {

@@ -120,6 +120,11 @@ int pair_exchange(int dtype, const void* orbitals, int n, const void* J, void* o
                   cudaStream_t s);
 // True when the plan's size has register-engine kernels (EPI_J available).
 bool poisson_j_supported(const PoissonPlan& pl);
+// True when energies take the spectral (Parseval) pass: FP64 plans on the
+// register engine. FP32 energies keep the full solves (their share of a mixed
+// SCF is small, and their rounding is the one the FP32 energy terms were
+// validated with).
+bool poisson_fe_supported(const PoissonPlan& pl);
 
 // Runs every field of `args` through the pair-solve pipeline in groups of
 // at most plan.max_fields. EPI_ACC: out[o] = (accumulate ? out[o] : 0) +

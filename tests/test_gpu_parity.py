@@ -362,11 +362,11 @@ def test_energy_terms_golden(dtype):
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_energy_spectral_pass_matches_full_solve(dtype):
-    """The energy pass sums ghat |F^|^2 over the spectrum (Parseval) instead of running the inverse
-    transforms. On the register engine it must agree with the full pair solves of the generic engine
+    """FP64 energies on the register engine sum ghat |F^|^2 over the spectrum (Parseval) instead of
+    running the inverse transforms; they must agree with the full pair solves of the generic engine
     for 1, 2 and 4 orbitals (1 orbital keeps the full solve: the split packing would double its
-    fields), on a grid whose x-pass CTAs do not tile the columns evenly (M = 48 with 32 lines per CTA
-    in FP32), and for the Hartree energy alone."""
+    fields), at two grid sizes (M = 48 and 64), and for the Hartree energy alone. FP32 energies keep
+    the full solves on both engines, which must agree as well."""
     from gato_gb300.autotune import set_plan
     from gato_gb300.grid import Grid3D
     from gato_gb300.scf import Operator, pair_fields
