@@ -9,6 +9,7 @@ import math
 
 import numpy as np
 import pytest
+import scipy.fft
 import scipy.special
 
 from oracle import gato_np as o
@@ -148,6 +149,24 @@ def test_hartree_linear_positive_and_scaling():      # test_poisson.py:60-90
     g = o.Grid3D(48, 10.0)
     ratio = o.hartree_energy(_gaussian(g, 2.0), g) / o.hartree_energy(_gaussian(g, 0.5), g)
     assert abs(ratio - 2.0) / 2.0 < 2e-2
+
+
+def test_spectral_energy_identity():
+    """The identity the FP64 energy pass rests on: the kernel spectrum is real and even, so for two
+    real densities packed as F = a + i b the kernel-weighted power of F's spectrum on the doubled
+    grid equals the sum of both Hartree-type energies (the cross terms cancel between k and -k)."""
+    g = o.Grid3D(12, 5.0)
+    N, M = g.N, 2 * g.N
+    rng = np.random.default_rng(3)
+    a, b = rng.standard_normal(g.shape), rng.standard_normal(g.shape)
+    Gh = scipy.fft.fftn(o._coulomb_kernel(N, g.h, g.h / 2))
+    assert np.max(np.abs(Gh.imag)) < 1e-9 * np.max(np.abs(Gh.real))
+    ghat = Gh.real * g.dV / M ** 3
+    F = np.zeros((M, M, M), complex)
+    F[:N, :N, :N] = a + 1j * b
+    spectral = g.dV * np.sum(ghat * np.abs(scipy.fft.fftn(F)) ** 2)
+    direct = o.integrate(a * o.hartree_potential(a, g), g) + o.integrate(b * o.hartree_potential(b, g), g)
+    assert abs(spectral - direct) < 1e-11 * abs(direct)
 
 
 # ---- lanczos (test_lanczos.py) ----------------------------------------------
