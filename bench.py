@@ -39,6 +39,12 @@ METRIC = "H2O 128^3 RHF block Fock-applies/s (mixed FP32/FP64 at |dE|<1uHa) and 
 UNIT = "Fock-applies/s"
 
 
+def workload_name(N: int, h: float) -> str:
+    """The bench workload, named the same on both arms."""
+    return (f"H2O HGH {N}^3 h={h} block Fock apply: 4 orbitals, 10 pair Poisson solves "
+            f"on the {2 * N}^3 doubled grid")
+
+
 def dist_env():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
             int(os.environ.get("LOCAL_RANK", 0)))
@@ -183,7 +189,8 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded water geometry and orbitals)",
-            "config": {"workload": f"H2O HGH {N}^3 h={h} block Fock apply, 4 orbitals, 10 pair Poisson solves"},
+            "config": {"workload": workload_name(N, h), "precision": "fp64", "N": N, "h": h, "n_occ": N_OCC,
+                       "parallelism": "rank 0 only (host cores)"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{args.steps} block Fock applies of the {N}^3 workload"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -533,8 +540,7 @@ def run_gato(args):
         "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded water geometry and orbitals)",
-        "config": {"workload": f"H2O HGH {N}^3 h={h} block Fock apply: 4 orbitals, 10 pair Poisson solves "
-                               f"on the {2 * N}^3 doubled grid", "precision": "mixed", "N": N, "h": h,
+        "config": {"workload": workload_name(N, h), "precision": "mixed", "N": N, "h": h,
                    "n_occ": N_OCC, "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas",
                    "autotune": tuned},
         "clocks": clk.summary(),
