@@ -186,8 +186,18 @@ def bo_energy_model(model, positions, charges, orbitals, grid: Grid3D, order: in
 
 
 def bo_grad_model(model, positions, charges, orbitals, grid: Grid3D, order: int = 4) -> torch.Tensor:
-    """dE/dR at fixed orbitals: the adjoint kernels alone."""
-    p = _t(positions).detach().clone().requires_grad_(True)
-    E = bo_energy_model(model, p, charges, orbitals, grid, order)
-    (g,) = torch.autograd.grad(E, p)
-    return g
+    """dE/dR at fixed orbitals (jax.grad of the BO energy in the reference): the adjoint kernels alone.
+
+    The position gradient of BOEnergy is its backward with dE/dE = 1, and it needs none of the
+    forward's energy terms (the kinetic, Hartree and exchange terms do not depend on R), so the
+    energy pass is skipped. The sum runs in the backward's order, so the result is the same.
+    ``order`` only enters the energy and is kept for the reference's signature."""
+    p = _t(positions)
+    fields = to_fields(orbitals)
+    nuclei = Nuclei(p.detach().to(torch.float64).cpu(), _t(charges))
+    g = model.v_ext_grad(nuclei, grid, _density_fields(fields))
+    nl = model.nonlocal_op(nuclei, grid, fields.dtype)
+    if nl is not None:
+        g = g + nl.grad(fields)
+    g = g + model.e_nn_grad(nuclei)
+    return g.to(dtype=p.dtype, device=p.device)

@@ -132,3 +132,48 @@ def test_grid_convergence_power_law_fit():
     e_inf, C, p, rms = fit_power_law(h, -17.3 + 2.0 * h ** 3.5)
     assert abs(e_inf + 17.3) < 1e-9 and abs(C - 2.0) < 1e-7 and abs(p - 3.5) < 1e-9 and rms < 1e-10
     assert all(math.isnan(v) for v in fit_power_law([0.2, 0.1], [1.0, 2.0]))
+
+
+def test_bo_gradient_composes_the_adjoint_terms(monkeypatch):
+    """The position gradient at fixed orbitals is the sum of the model's adjoint terms (local
+    potential, non-local projectors when the model has them, nuclear repulsion) in the adjoint's
+    order, returned in the positions' dtype; no energy term is evaluated for it."""
+    import torch
+    from gato_gb300.grid import Grid3D
+    from gato_gb300.physics import _molecule as mol
+
+    calls = []
+    monkeypatch.setattr(mol, "to_fields", lambda orb: orb.permute(3, 0, 1, 2))
+    monkeypatch.setattr(mol, "_density_fields", lambda f: 2 * (f * f).sum(0))
+    monkeypatch.setattr(mol, "_energy_terms", lambda *a, **k: calls.append("energy"))
+
+    class NL:
+        def grad(self, fields):
+            calls.append("nl")
+            return torch.full((2, 3), 0.25, dtype=torch.float64)
+
+    class Model:
+        def __init__(self, with_nl):
+            self.with_nl = with_nl
+
+        def v_ext_grad(self, nuclei, grid, rho):
+            calls.append("v_ext")
+            assert nuclei.positions.dtype == torch.float64 and rho.shape == (4, 4, 4)
+            return torch.full((2, 3), float(rho.sum()), dtype=torch.float64)
+
+        def nonlocal_op(self, nuclei, grid, dtype):
+            return NL() if self.with_nl else None
+
+        def e_nn_grad(self, nuclei):
+            calls.append("e_nn")
+            return torch.ones((2, 3), dtype=torch.float64)
+
+    orb = torch.ones((4, 4, 4, 1), dtype=torch.float64)
+    pos = torch.zeros((2, 3), dtype=torch.float32)
+    g = mol.bo_grad_model(Model(True), pos, [1.0, 1.0], orb, Grid3D(4, 2.0))
+    assert g.dtype == torch.float32 and torch.allclose(g, torch.full((2, 3), 128.0 + 0.25 + 1.0))
+    assert calls == ["v_ext", "nl", "e_nn"]
+    calls.clear()
+    g = mol.bo_grad_model(Model(False), pos.double(), [1.0, 1.0], orb, Grid3D(4, 2.0))
+    assert g.dtype == torch.float64 and torch.allclose(g, torch.full((2, 3), 129.0, dtype=torch.float64))
+    assert calls == ["v_ext", "e_nn"]
