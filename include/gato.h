@@ -131,7 +131,10 @@ int gato_poisson_create(int dtype, int N, double h, double eps, int max_fields,
 int gato_poisson_destroy(gato_poisson_t plan);
 /* J = hartree_potential(rho): poisson.py:47-79.                           */
 int gato_hartree_potential(gato_poisson_t plan, const void* rho, void* J, void* stream);
-/* E_dev[0] = 0.5 * dV * sum rho J[rho]: poisson.py:82-92.                 */
+/* E_dev[0] = 0.5 * dV * sum rho J[rho]: poisson.py:82-92. FP64 plans on the
+ * register engine evaluate it from the spectrum, 0.5 * dV * sum_k ghat |rho^|^2
+ * (Parseval on the doubled grid, equal in exact arithmetic), without the
+ * inverse transforms.                                                      */
 int gato_hartree_energy(gato_poisson_t plan, const void* rho, double* E_dev, void* stream);
 /* Profiling hook (no reference counterpart): runs stage 1 (y forward),
  * 2 (x forward, kernel multiply, x inverse) or 3 (y inverse) of the pair-
@@ -187,7 +190,10 @@ int gato_op_apply(gato_op_t op, const void* in, void* out, void* stream);
 int gato_op_apply_block(gato_op_t op, void* out, void* stream);
 /* terms_dev[0..4] = (kinetic, v_ext, v_nl, hartree, exchange) of
  * decompose_rhf_energy (scf.py:194-265) for the operator's orbitals,
- * with v_ext taken against V_ext_dev (the operator's V may hold V_H).   */
+ * with v_ext taken against V_ext_dev (the operator's V may hold V_H).
+ * Hartree and exchange come from one batched pass over the density and the
+ * pair densities; FP64 operators take it in the spectral form of
+ * gato_hartree_energy.                                                    */
 int gato_op_energy_terms(gato_op_t op, const void* V_ext, double* terms_dev, void* stream);
 
 /* ---- solvers/lanczos.py ----------------------------------------------------
