@@ -52,7 +52,10 @@ typedef struct gato_poisson_plan* gato_poisson_t;
 typedef struct gato_nonlocal* gato_nonlocal_t;
 typedef struct gato_operator* gato_op_t;
 
-/* ---- library ------------------------------------------------------------ */
+/* ---- library ------------------------------------------------------------
+ * Library services with no reference counterpart (the reference is Python
+ * and reports errors as exceptions, which the Python layer raises from the
+ * status and this message).                                                */
 int gato_version(void);
 int gato_last_error(char* buf, size_t len);
 /* Reads and clears the device error word set by bounded spin-waits. */
@@ -114,6 +117,8 @@ int gato_nonlocal_create(int dtype, int N, double L, int K, const double* pos_ho
                          const int* nch_host, const int* ell_host, const double* r_host,
                          const int* n_host, const double* h_host, double cut_sigmas,
                          gato_nonlocal_t* out);
+/* Frees the projector set (no reference counterpart: the reference
+ * rebuilds the projector fields on every apply).                          */
 int gato_nonlocal_destroy(gato_nonlocal_t nl);
 /* out[b] += V_nl psi[b] for b < nb: hgh_nonlocal_apply (pseudopotentials.py:360-383). */
 int gato_nonlocal_apply(gato_nonlocal_t nl, const void* psi, void* out, int nb, void* stream);
@@ -158,7 +163,8 @@ int gato_mix(int dtype, void* rho, const void* rho_new, int64_t npts, double a, 
 int gato_axpby(int dtype, const void* x, const void* y, void* out, int64_t npts, double a, double b,
                void* stream);
 /* dst = (dst dtype) src, n elements: the precision changes between the FP32
- * Fock applies and the FP64 density / Hartree / energy of the mixed SCF.    */
+ * Fock applies and the FP64 density / Hartree / energy of the mixed SCF.
+ * No reference counterpart: the reference computes in FP64 throughout.     */
 int gato_convert(int src_dtype, const void* src, int dst_dtype, void* dst, int64_t n, void* stream);
 /* out_dev[0] = scale * sum_i a_i w_i b_i: <psi|V|psi> of potential_energy
  * (observables.py:26-30).                                                  */
@@ -244,6 +250,8 @@ int gato_radial_density(int dtype, const void* re, const void* im, int N, double
 int gato_hgh_local_grad(int dtype, const void* rho, int N, double L, int K, const double* pos_host,
                         const double* Zion_host, const double* rloc_host, const double* c_host,
                         double* grad_host, void* stream);
+/* The projector term alone: 2 sum_i <phi_i|V_nl(R)|phi_i> differentiated
+ * in R (pseudopotentials.py:330-383 under water.py:221-241's jax.grad).   */
 int gato_nonlocal_grad(gato_nonlocal_t nl, const void* orbitals, int n, double* grad_host, void* stream);
 /* grad_host (K*3) += d/dR of int rho V_ext for the multi-centre softened
  * Coulomb V_ext = -sum_k Z_k / sqrt(|r - R_k|^2 + eps^2) (potentials.py:39-61);
