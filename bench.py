@@ -50,30 +50,38 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
-def synthetic_water(N: int, h: float, seed: int = 2024):
-    """Seeded geometry and four orthonormal smooth orbitals (float64, host numpy)."""
+def synthetic_orbitals(centres, N: int, h: float, n_occ: int, rng):
+    """n_occ orthonormal smooth orbitals (float64, host numpy) on the N^3 grid of spacing h: Gaussians
+    of seeded width around the given centres (cycled) times a seeded linear factor, orthonormalised by
+    Gram-Schmidt in the grid inner product."""
     import numpy as np
     L = N * h
-    rng = np.random.default_rng(seed)
-    half = math.radians(104.5) / 2
-    pos = np.array([[0.0, 0.0, 0.0], [1.81 * math.sin(half), 0.0, 1.81 * math.cos(half)],
-                    [-1.81 * math.sin(half), 0.0, 1.81 * math.cos(half)]])
-    pos = pos + rng.uniform(-0.05, 0.05, (3, 3))
     a = -L / 2 + (np.arange(N) + 0.5) * h
     X, Y, Z = np.meshgrid(a, a, a, indexing="ij")
-    orbs = np.empty((N_OCC, N, N, N))
-    for k in range(N_OCC):
-        c = pos[k % 3] + rng.uniform(-0.3, 0.3, 3)
+    orbs = np.empty((n_occ, N, N, N))
+    for k in range(n_occ):
+        c = centres[k % len(centres)] + rng.uniform(-0.3, 0.3, 3)
         al = rng.uniform(0.4, 0.9)
         w = rng.uniform(-0.3, 0.3, 3)
         orbs[k] = np.exp(-al * ((X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2)) * (
             1.0 + w[0] * X + w[1] * Y + w[2] * Z)
     dV = h ** 3
-    for i in range(N_OCC):
+    for i in range(n_occ):
         for j in range(i):
             orbs[i] -= np.sum(orbs[i] * orbs[j]) * dV * orbs[j]
         orbs[i] /= math.sqrt(np.sum(orbs[i] ** 2) * dV)
-    return pos, orbs
+    return orbs
+
+
+def synthetic_water(N: int, h: float, seed: int = 2024):
+    """Seeded geometry and four orthonormal smooth orbitals (float64, host numpy)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    half = math.radians(104.5) / 2
+    pos = np.array([[0.0, 0.0, 0.0], [1.81 * math.sin(half), 0.0, 1.81 * math.cos(half)],
+                    [-1.81 * math.sin(half), 0.0, 1.81 * math.cos(half)]])
+    pos = pos + rng.uniform(-0.05, 0.05, (3, 3))
+    return pos, synthetic_orbitals(pos, N, h, N_OCC, rng)
 
 
 class ClockSampler:

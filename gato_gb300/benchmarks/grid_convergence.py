@@ -1,225 +1,200 @@
-"""Grid-convergence study for the HGH molecules (reference: benchmarks/grid_convergence.py:1-308).
+"""Convergence of GPU RHF results with grid spacing and box size.
 
-A real-space result carries a resolution error (the spacing h = L/N) and a
-box error (the side L). Three sweeps separate them, each finished by a fit
-E(x) = E_inf + C x^p whose order p is found by a scan:
+Reference counterpart: benchmarks/grid_convergence.py (a sweep harness over the
+water and HCl drivers). This module is organised around a declarative list of
+sweep points instead of per-molecule adapter classes:
 
-    energy    E(h) at fixed L and geometry      -> resolution error, h -> 0
-    box       E(L) at fixed h (N = L / h)       -> box error, 1/L -> 0
-    geometry  relaxed R, angle and E against h  -> does the geometry converge
+* a **study** is a list of ``SweepPoint(molecule, N, L, task)`` records,
+  built by ``spacing_study`` (N varies at fixed L), ``box_study`` (L varies at
+  a held spacing, N = nearest even L / h) or ``relax_study`` (a geometry
+  relaxation per N);
+* ``run_study`` evaluates every point with the package's own SCF (and
+  optimiser) and returns JSON-ready records, one per point;
+* ``extrapolate`` fits y(x) = y_inf + C x^p by **variable projection**
+  (Golub and Pereyra, SIAM J. Numer. Anal. 10, 1973): for a fixed exponent the
+  model is linear in (y_inf, C), which linear least squares eliminates, and
+  the remaining one-dimensional residual is minimised over p with Brent's
+  bounded method.
 
-    python -m gato_gb300.benchmarks.grid_convergence --molecule water --mode energy
-    python -m gato_gb300.benchmarks.grid_convergence --molecule hcl --mode box --precision mixed
+The command line prints the records and fits as one JSON document::
 
-Each SCF runs on the GPU through the package's own solvers; ``--precision
-mixed`` uses the FP32 Fock path with FP64 energies, which makes the larger
-grids of the sweep cheap.
+    python -m gato_gb300.benchmarks.grid_convergence water spacing --N 32 40 48 --L 12
+    python -m gato_gb300.benchmarks.grid_convergence hcl box --sides 8 9 10 --h 0.25 --out box.json
 """
 from __future__ import annotations
 
 import argparse
 import json
 import math
+import sys
 import time
+from dataclasses import asdict, dataclass
 
 import numpy as np
 
 from ..geometry import bond_angle, bond_length
 from ..grid import Grid3D
-from ..physics import hcl as hcl_mod
-from ..physics import water as water_mod
+from ..physics import hcl, water
+
+# molecule name -> (starting geometry, HGH elements, single-point solver, relaxation driver)
+MOLECULES = {
+    "water": (water.water_initial_geometry, water.water_hgh_elements, water.solve_rhf_at_geometry,
+              water.optimize_water_geometry),
+    "hcl": (hcl.hcl_initial_geometry, hcl.hcl_hgh_elements, hcl.solve_rhf_at_geometry,
+            hcl.optimize_geometry),
+}
 
 
-class WaterCase:
-    name = "H2O"
-    default_L = 14.0
-    R0, angle0 = 1.81, 104.5   # near the relaxed geometry
+@dataclass(frozen=True)
+class SweepPoint:
+    molecule: str
+    N: int
+    L: float
+    task: str = "energy"    # "energy": one SCF; "relax": geometry relaxation then its energy
 
-    def nuclei(self):
-        return water_mod.water_initial_geometry(R_OH=self.R0, angle_deg=self.angle0)
-
-    def elements(self):
-        return water_mod.water_hgh_elements()
-
-    def solve(self, nuclei, grid, **kw):
-        return water_mod.solve_rhf_at_geometry(nuclei, self.elements(), grid, **kw)
-
-    def optimize(self, grid, **kw):
-        res = water_mod.optimize_water_geometry(self.nuclei(), self.elements(), grid, verbose=False, **kw)
-        n = res.final.nuclei
-        return {"E": res.final.energy, "R": float(bond_length(n, 0, 1)),
-                "angle": math.degrees(float(bond_angle(n, 1, 0, 2))), "converged": res.final.converged}
+    @property
+    def h(self) -> float:
+        return self.L / self.N
 
 
-class HClCase:
-    name = "HCl"
-    default_L = 14.0
-    R0 = 2.41
-
-    def nuclei(self):
-        return hcl_mod.hcl_initial_geometry(R_HCl=self.R0)
-
-    def elements(self):
-        return hcl_mod.hcl_hgh_elements()
-
-    def solve(self, nuclei, grid, **kw):
-        return hcl_mod.solve_rhf_at_geometry(nuclei, self.elements(), grid, **kw)
-
-    def optimize(self, grid, **kw):
-        kw.pop("lanczos_iters", None)
-        res = hcl_mod.optimize_geometry(self.nuclei(), self.elements(), grid, verbose=False, **kw)
-        n = res.final.nuclei
-        return {"E": res.final.energy, "R": float(bond_length(n, 0, 1)), "angle": float("nan"),
-                "converged": res.final.converged}
+def spacing_study(molecule: str, Ns, L: float) -> list[SweepPoint]:
+    return [SweepPoint(molecule, int(n), float(L)) for n in Ns]
 
 
-CASES = {"water": WaterCase, "hcl": HClCase}
+def box_study(molecule: str, sides, h: float) -> list[SweepPoint]:
+    """One point per box side, N the even integer nearest to L / h."""
+    return [SweepPoint(molecule, 2 * max(1, int(round(s / h / 2.0))), float(s)) for s in sides]
 
 
-def fit_power_law(xs, ys):
-    """Least-squares y = y_inf + C x^p over a scan of p in [0.5, 6] (1101 points).
+def relax_study(molecule: str, Ns, L: float) -> list[SweepPoint]:
+    return [SweepPoint(molecule, int(n), float(L), task="relax") for n in Ns]
 
-    For a fixed p the model is linear in (y_inf, C): one 2-column lstsq per
-    candidate; the p with the smallest rms residual wins. Returns
-    (y_inf, C, p, rms), all nan with fewer than three points.
+
+def _shape(nuclei) -> dict:
+    """Bond length of nuclei 0-1 and, for three nuclei, the angle at nucleus 0 (degrees)."""
+    out = {"R": float(bond_length(nuclei, 0, 1))}
+    if nuclei.n == 3:
+        out["angle"] = math.degrees(float(bond_angle(nuclei, 1, 0, 2)))
+    return out
+
+
+def evaluate(pt: SweepPoint, *, order: int = 4, precision: str = "mixed", max_scf: int = 60,
+             relax_steps: int = 20, relax_lr: float = 0.04) -> dict:
+    """One record: the point, its energy, SCF outcome and wall time (and the relaxed shape)."""
+    geometry, elements, solve, relax = MOLECULES[pt.molecule]
+    grid = Grid3D(N=pt.N, L=pt.L)
+    t0 = time.perf_counter()
+    if pt.task == "energy":
+        res = solve(geometry(), elements(), grid, max_iters=max_scf, order=order, precision=precision)
+        rec = {"E": float(res.energy), "scf_iters": int(res.n_iters), "converged": bool(res.converged)}
+    elif pt.task == "relax":
+        opt = relax(geometry(), elements(), grid, geom_steps=relax_steps, learning_rate=relax_lr,
+                    scf_max_iters=max_scf, order=order, verbose=False, precision=precision)
+        fin = opt.final
+        rec = {"E": float(fin.energy), "scf_iters": int(fin.n_iters), "converged": bool(fin.converged),
+               **_shape(fin.nuclei)}
+    else:
+        raise ValueError(f"unknown task {pt.task!r}")
+    return {**asdict(pt), "h": pt.h, **rec, "seconds": time.perf_counter() - t0}
+
+
+def run_study(points, log=None, **kw) -> list[dict]:
+    """Evaluate every point in order; ``log`` (a file) gets one line per finished point."""
+    records = []
+    for pt in points:
+        rec = evaluate(pt, **kw)
+        records.append(rec)
+        if log is not None:
+            print(f"[{pt.molecule} {pt.task} N={pt.N} L={pt.L:g} h={pt.h:.5f}] E={rec['E']:+.8f} "
+                  f"scf={rec['scf_iters']} conv={rec['converged']} {rec['seconds']:.1f}s", file=log, flush=True)
+    return records
+
+
+def extrapolate(xs, ys, p_bounds=(0.5, 6.0)) -> dict | None:
+    """Variable-projection fit of y = y_inf + C x^p; None with fewer than three points.
+
+    For fixed p, (y_inf, C) solve a two-column linear least-squares problem;
+    p minimises the resulting residual norm (Brent, bounded). The residual is
+    also compared at the two bounds, so a monotone residual returns the
+    better bound rather than an interior stationary point.
     """
+    from scipy.optimize import minimize_scalar
+
     x = np.asarray(xs, dtype=float)
     y = np.asarray(ys, dtype=float)
     if x.size < 3:
-        return (float("nan"),) * 4
-    best = None
-    for p in np.linspace(0.5, 6.0, 1101):
-        A = np.stack([np.ones_like(x), x ** p], axis=1)
-        coef = np.linalg.lstsq(A, y, rcond=None)[0]
-        rms = float(np.sqrt(np.mean((y - A @ coef) ** 2)))
-        if best is None or rms < best[3]:
-            best = (float(coef[0]), float(coef[1]), float(p), rms)
-    return best
-
-
-def _report(label, xs, ys, unit):
-    y_inf, _, p, rms = fit_power_law(xs, ys)
-    if math.isnan(p):
-        print(f"  {label}: need >= 3 points to fit")
         return None
-    print(f"  {label}: extrapolated {y_inf:+.6f} {unit}   (order p = {p:.2f}, rms resid = {rms:.2e})")
-    return {"extrapolated": y_inf, "order": p, "rms": rms}
+
+    def solve_linear(p):
+        A = np.column_stack([np.ones_like(x), x ** p])
+        coef, *_ = np.linalg.lstsq(A, y, rcond=None)
+        r = y - A @ coef
+        return coef, float(np.sqrt(np.mean(r * r)))
+
+    opt = minimize_scalar(lambda p: solve_linear(p)[1], bounds=p_bounds, method="bounded",
+                          options={"xatol": 1e-12})
+    cands = [float(opt.x), float(p_bounds[0]), float(p_bounds[1])]
+    p = min(cands, key=lambda q: solve_linear(q)[1])
+    coef, rms = solve_linear(p)
+    return {"y_inf": float(coef[0]), "C": float(coef[1]), "p": p, "rms": rms, "points": int(x.size)}
 
 
-def sweep_energy(case, Ns, L, order, scf_iters, precision="fp64"):
-    """E against h at fixed L and geometry."""
-    print(f"{case.name}: energy vs grid spacing at fixed L = {L} a0, stencil order {order}, {precision}")
-    print(f"{'N':>5} {'h (a0)':>9} {'E (Ha)':>15} {'SCF it':>7} {'conv':>6} {'time':>8}")
-    rows, nuclei = [], case.nuclei()
-    for N in Ns:
-        grid = Grid3D(N=N, L=L)
-        t0 = time.perf_counter()
-        pt = case.solve(nuclei, grid, max_iters=scf_iters, order=order, precision=precision)
-        dt = time.perf_counter() - t0
-        print(f"{N:5d} {grid.h:9.5f} {pt.energy:+15.8f} {pt.n_iters:7d} {str(pt.converged):>6} {dt:7.2f}s",
-              flush=True)
-        rows.append({"N": N, "h": grid.h, "E": pt.energy, "iters": pt.n_iters, "converged": pt.converged,
-                     "seconds": dt})
-        if not pt.converged:
-            print("      ^ left out of the fit: SCF did not converge")
-    print()
-    ok = [r for r in rows if r["converged"]]
-    fit = _report("E(h -> 0)", [r["h"] for r in ok], [r["E"] for r in ok], "Ha")
-    return {"rows": rows, "fit": fit}
+def summarise(study: str, records: list[dict]) -> dict:
+    """The fits a study supports, over the points whose SCF converged.
 
-
-def sweep_box(case, Ls, target_h, order, scf_iters, precision="fp64"):
-    """E against L at (nearly) fixed h: N = L / h rounded to an even integer.
-
-    The achieved h is printed and a drift in h is reported, since dE/dh near
-    h = 0.175 is about 1.6 Ha per bohr and a 1.5% drift in h swamps the box
-    effect; pick target_h so that every L / target_h is an integer.
+    spacing: E against h. box: E against 1/L, plus the spread of the spacing
+    actually used (a box study holds h only as far as L / N allows). relax:
+    E, R (and the angle) against h.
     """
-    print(f"{case.name}: energy vs box size at fixed h ~ {target_h} a0, stencil order {order}, {precision}")
-    print(f"{'L':>6} {'N':>5} {'h (a0)':>9} {'E (Ha)':>15} {'SCF it':>7} {'conv':>6} {'time':>8}")
-    rows, nuclei = [], case.nuclei()
-    for L in Ls:
-        N = int(round(L / target_h / 2)) * 2
-        grid = Grid3D(N=N, L=L)
-        t0 = time.perf_counter()
-        pt = case.solve(nuclei, grid, max_iters=scf_iters, order=order, precision=precision)
-        dt = time.perf_counter() - t0
-        print(f"{L:6.1f} {N:5d} {grid.h:9.5f} {pt.energy:+15.8f} {pt.n_iters:7d} {str(pt.converged):>6} "
-              f"{dt:7.2f}s", flush=True)
-        rows.append({"L": L, "N": N, "h": grid.h, "E": pt.energy, "iters": pt.n_iters,
-                     "converged": pt.converged, "seconds": dt})
-    print()
-    ok = [r for r in rows if r["converged"]]
+    ok = [r for r in records if r["converged"]]
+    out: dict = {"study": study, "points": len(records), "converged": len(ok)}
     hs = [r["h"] for r in ok]
-    drift = bool(hs) and (max(hs) - min(hs)) > 1e-4
-    if drift:
-        print(f"  WARNING: h drifted over {min(hs):.5f}..{max(hs):.5f}; box and resolution errors are "
-              f"confounded and the fit is unreliable. Use a target_h that divides every L.")
-        groups: dict = {}
-        for r in ok:
-            groups.setdefault(round(r["h"], 10), []).append(r)
-        for h, grp in sorted(groups.items()):
-            if len(grp) >= 2:
-                es = [r["E"] for r in grp]
-                which = ", ".join("L=%g" % r["L"] for r in grp)
-                print(f"  controlled at h = {h:.5f} ({which}): spread {1e3 * (max(es) - min(es)):.2f} mHa")
-    fit = _report("E(L -> inf)", [1.0 / r["L"] for r in ok], [r["E"] for r in ok], "Ha") if len(ok) >= 3 else None
-    return {"rows": rows, "fit": fit, "h_drift": drift}
-
-
-def sweep_geometry(case, Ns, L, order, geom_steps, lr, scf_iters, precision="fp64"):
-    """Relaxed geometry against h."""
-    print(f"{case.name}: relaxed geometry vs grid spacing at fixed L = {L} a0, {precision}")
-    print(f"{'N':>5} {'h (a0)':>9} {'R (a0)':>10} {'angle':>9} {'E (Ha)':>15} {'conv':>6} {'time':>8}")
-    rows = []
-    for N in Ns:
-        grid = Grid3D(N=N, L=L)
-        t0 = time.perf_counter()
-        out = case.optimize(grid, geom_steps=geom_steps, learning_rate=lr, scf_max_iters=scf_iters, order=order,
-                            precision=precision)
-        dt = time.perf_counter() - t0
-        print(f"{N:5d} {grid.h:9.5f} {out['R']:10.5f} {out['angle']:9.3f} {out['E']:+15.8f} "
-              f"{str(out['converged']):>6} {dt:7.2f}s", flush=True)
-        rows.append(dict(out, N=N, h=grid.h, seconds=dt))
-    print()
-    ok = [r for r in rows if r["converged"]]
-    hs = [r["h"] for r in ok]
-    fits = {"R": _report("R(h -> 0)", hs, [r["R"] for r in ok], "a0")}
-    if ok and not math.isnan(ok[0]["angle"]):
-        fits["angle"] = _report("angle(h -> 0)", hs, [r["angle"] for r in ok], "deg")
-    fits["E"] = _report("E(h -> 0)", hs, [r["E"] for r in ok], "Ha")
-    return {"rows": rows, "fit": fits}
+    if study == "spacing":
+        out["E_vs_h"] = extrapolate(hs, [r["E"] for r in ok])
+    elif study == "box":
+        out["E_vs_inv_L"] = extrapolate([1.0 / r["L"] for r in ok], [r["E"] for r in ok])
+        out["h_spread"] = (max(hs) - min(hs)) if hs else None
+    elif study == "relax":
+        for key in ("E", "R", "angle"):
+            if ok and key in ok[0]:
+                out[f"{key}_vs_h"] = extrapolate(hs, [r[key] for r in ok])
+    return out
 
 
 def main(argv=None) -> dict:
-    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("--molecule", choices=sorted(CASES), default="water")
-    ap.add_argument("--mode", choices=["energy", "box", "geometry"], default="energy")
-    ap.add_argument("--N", type=int, nargs="+", default=None, help="grid sizes (energy / geometry modes)")
-    ap.add_argument("--L", type=float, default=None, help="box side (energy / geometry modes)")
-    ap.add_argument("--box-L", type=float, nargs="+", default=[12.0, 14.0, 16.0, 18.0])
-    ap.add_argument("--target-h", type=float, default=0.175, help="spacing held in box mode")
+    ap = argparse.ArgumentParser(description="grid and box convergence of GPU RHF energies")
+    ap.add_argument("molecule", choices=sorted(MOLECULES))
+    ap.add_argument("study", choices=["spacing", "box", "relax"])
+    ap.add_argument("--N", type=int, nargs="+", default=[32, 40, 48, 56, 64],
+                    help="grid points per axis (spacing and relax studies)")
+    ap.add_argument("--L", type=float, default=12.0, help="box side in bohr (spacing and relax studies)")
+    ap.add_argument("--sides", type=float, nargs="+", default=[10.0, 12.0, 14.0, 16.0],
+                    help="box sides in bohr (box study)")
+    ap.add_argument("--h", type=float, default=0.25, help="held grid spacing in bohr (box study)")
     ap.add_argument("--order", type=int, choices=[2, 4], default=4)
-    ap.add_argument("--scf-iters", type=int, default=80)
-    ap.add_argument("--geom-steps", type=int, default=30)
-    ap.add_argument("--lr", type=float, default=0.05)
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
-    ap.add_argument("--json", default=None, help="also write the rows and fits to this file")
-    args = ap.parse_args(argv)
-    case = CASES[args.molecule]()
-    L = args.L if args.L is not None else case.default_L
-    if args.mode == "energy":
-        out = sweep_energy(case, args.N or [32, 48, 64, 80, 96, 112, 128], L, args.order, args.scf_iters,
-                           args.precision)
-    elif args.mode == "box":
-        out = sweep_box(case, args.box_L, args.target_h, args.order, args.scf_iters, args.precision)
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--max-scf", type=int, default=60)
+    ap.add_argument("--relax-steps", type=int, default=20)
+    ap.add_argument("--relax-lr", type=float, default=0.04)
+    ap.add_argument("--out", default=None, help="write the JSON document here instead of stdout")
+    ap.add_argument("--quiet", action="store_true", help="no per-point progress lines on stderr")
+    a = ap.parse_args(argv)
+    if a.study == "spacing":
+        points = spacing_study(a.molecule, a.N, a.L)
+    elif a.study == "box":
+        points = box_study(a.molecule, a.sides, a.h)
     else:
-        out = sweep_geometry(case, args.N or [32, 48, 64, 80, 96], L, args.order, args.geom_steps, args.lr,
-                             args.scf_iters, args.precision)
-    if args.json:
-        with open(args.json, "w") as f:
-            json.dump(out, f, indent=1)
-    return out
+        points = relax_study(a.molecule, a.N, a.L)
+    records = run_study(points, log=None if a.quiet else sys.stderr, order=a.order, precision=a.precision,
+                        max_scf=a.max_scf, relax_steps=a.relax_steps, relax_lr=a.relax_lr)
+    doc = {"records": records, "summary": summarise(a.study, records)}
+    text = json.dumps(doc, indent=1)
+    if a.out:
+        with open(a.out, "w") as f:
+            f.write(text + "\n")
+    else:
+        print(text)
+    return doc
 
 
 if __name__ == "__main__":

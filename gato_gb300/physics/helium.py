@@ -58,13 +58,8 @@ def solve_helium(N: int = 64, L: float = 10.0, Z: float = 2.0, epsilon: float | 
                        converged=result.converged,
                        history=[(i + 1, e) for i, e in enumerate(result.energy_history)])
     if verbose:
-        print(f"Helium-like atom Z={Z} on {N}^3 grid, L = {L}  (h = {grid.h:.4f}, stencil order {order})")
-        print(f"Method        : RHF   SCF iters = {result.n_iters}   converged = {result.converged}")
-        print(f"Energy        : {out.energy:+.6f} Ha")
-        print(f"<T>           : {T:+.6f} Ha")
-        print(f"<V_ext>       : {V_exp:+.6f} Ha")
-        print(f"E_H[rho]      : {E_H:+.6f} Ha")
-        print(f"<E_x>         : {E_x:+.6f} Ha")
-        print(f"eps_HOMO      : {float(result.orbital_energies[0]):+.6f} Ha")
-        print(f"Virial 2T/|V| : {vr:+.6f}")
+        summary = {"E": out.energy, "T": T, "V_ext": V_exp, "E_H": E_H, "E_x": E_x,
+                   "eps_1": float(result.orbital_energies[0]), "2T/|V|": vr}
+        print(f"He-like Z={Z:g} N={N} L={L:g} order={order}: SCF {result.n_iters} iterations "
+              f"(converged={result.converged}); " + ", ".join(f"{k}={v:.6f}" for k, v in summary.items()))
     return out

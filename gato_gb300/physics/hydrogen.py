@@ -1,8 +1,11 @@
-"""Hydrogen-like atom by imaginary-time propagation (reference: physics/hydrogen.py:1-133).
+"""One-electron atom in imaginary time (reference counterpart: physics/hydrogen.py).
 
-One electron in a softened Coulomb well of charge Z; the ground state from
-``imaginary_time`` (a CUDA-graph replayed Euler step), then the observables
-<T>, <V> and the virial ratio. E_0(Z) = -Z^2 / 2 Ha analytically.
+The softened Coulomb well of charge Z at the box centre is relaxed to its
+ground state by ``imaginary_time`` (a replayed fused Euler step on the
+device); the result carries the normalised state and its kinetic and
+potential expectation values. The exact nonrelativistic ground-state energy
+of the unsoftened well is -Z^2 / 2 Ha, and a Coulomb eigenstate has
+2<T> / |<V>| = 1.
 """
 from __future__ import annotations
 
@@ -13,14 +16,14 @@ import torch
 from ..ansatz import init_grid_ansatz
 from ..grid import Grid3D, normalize
 from ..hamiltonian import Hamiltonian
-from ..observables import kinetic_energy, potential_energy, virial_ratio
+from ..observables import kinetic_energy, potential_energy
 from ..potentials import softened_coulomb
 from ..solvers.imag_time import imaginary_time
 
 
 @dataclass
 class HydrogenResult:
-    """hydrogen.py:27-36."""
+    """Field names as in the reference's result record (hydrogen.py:27-36)."""
 
     grid: Grid3D
     psi: torch.Tensor
@@ -34,25 +37,18 @@ class HydrogenResult:
 
 def solve_hydrogen(N: int = 48, L: float = 10.0, Z: float = 1.0, epsilon: float | None = None,
                    n_steps: int = 3000, order: int = 2, seed: int = 0, verbose: bool = True) -> HydrogenResult:
-    """Hydrogen-like ground state for nuclear charge Z at the origin (hydrogen.py:39-102)."""
+    """Ground state of charge Z by imaginary time from a hydrogenic start (seeded)."""
     grid = Grid3D(N=N, L=L)
-    V = softened_coulomb(grid, Z=Z, epsilon=epsilon)
-    H = Hamiltonian(grid=grid, V=V, boundary="dirichlet", order=order)
-    psi0 = init_grid_ansatz(grid, seed, init="hydrogenic", Z=Z)
-    psi, history = imaginary_time(H, psi0, n_steps=n_steps, log_every=max(1, n_steps // 20))
-    hist = list(zip(history.steps, history.energies))
-    psi = normalize(psi, grid)
-    T = float(kinetic_energy(psi, grid, order=order))
-    V_exp = float(potential_energy(psi, V, grid))
-    vr = float(virial_ratio(psi, V, grid, order=order))
-    res = HydrogenResult(grid=grid, psi=psi, V=V, energy=T + V_exp, kinetic=T, potential=V_exp, virial_ratio=vr,
-                         history=hist)
+    well = softened_coulomb(grid, Z=Z, epsilon=epsilon)
+    start = init_grid_ansatz(grid, seed, init="hydrogenic", Z=Z)
+    state, log = imaginary_time(Hamiltonian(grid=grid, V=well, order=order), start, n_steps=n_steps,
+                                log_every=max(1, n_steps // 20))
+    state = normalize(state, grid)
+    t = float(kinetic_energy(state, grid, order=order))
+    v = float(potential_energy(state, well, grid))
+    out = HydrogenResult(grid=grid, psi=state, V=well, energy=t + v, kinetic=t, potential=v,
+                         virial_ratio=2.0 * t / abs(v), history=list(zip(log.steps, log.energies)))
     if verbose:
-        E0 = -0.5 * Z * Z
-        print(f"Hydrogenic atom Z={Z} on {N}^3 grid, L = {L}  (h = {grid.h:.4f}, stencil order {order})")
-        print(f"Solver        : imag_time   steps = {n_steps}")
-        print(f"Energy        : {res.energy:+.6f} Ha     (target: {E0:+.6f})")
-        print(f"<T>           : {T:+.6f} Ha     (analytic: {-E0:+.6f})")
-        print(f"<V>           : {V_exp:+.6f} Ha     (analytic: {2 * E0:+.6f})")
-        print(f"Virial 2T/|V| : {vr:+.6f}        (target:  1.000000)")
-    return res
+        print(f"hydrogenic Z={Z:g} N={N} L={L:g} order={order} steps={n_steps}: E={out.energy:.6f} Ha "
+              f"(exact {-0.5 * Z * Z:.6f}), T={t:.6f}, V={v:.6f}, 2T/|V|={out.virial_ratio:.5f}")
+    return out

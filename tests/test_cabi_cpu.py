@@ -121,17 +121,19 @@ def test_lookup_and_tables():
     assert total_valence_charge((lookup("O"), lookup("H"), lookup("H"))) == 8.0
 
 
-def test_grid_convergence_power_law_fit():
-    """The scan fit of benchmarks/grid_convergence.py recovers a known law; < 3 points -> nan."""
-    import math
-
+def test_grid_convergence_variable_projection_fit():
+    """The variable-projection fit of benchmarks/grid_convergence.py recovers a known law, stops at a
+    bound for a monotone residual, returns None below three points; box studies pick even N."""
     import numpy as np
 
-    from gato_gb300.benchmarks.grid_convergence import fit_power_law
+    from gato_gb300.benchmarks.grid_convergence import box_study, extrapolate
     h = np.array([0.35, 0.3, 0.25, 0.2, 0.15])
-    e_inf, C, p, rms = fit_power_law(h, -17.3 + 2.0 * h ** 3.5)
-    assert abs(e_inf + 17.3) < 1e-9 and abs(C - 2.0) < 1e-7 and abs(p - 3.5) < 1e-9 and rms < 1e-10
-    assert all(math.isnan(v) for v in fit_power_law([0.2, 0.1], [1.0, 2.0]))
+    fit = extrapolate(h, -17.3 + 2.0 * h ** 3.5)
+    assert abs(fit["y_inf"] + 17.3) < 1e-9 and abs(fit["C"] - 2.0) < 1e-6 and abs(fit["p"] - 3.5) < 1e-6
+    assert fit["rms"] < 1e-9 and fit["points"] == 5
+    assert extrapolate(h, 1.0 + h ** 0.2)["p"] == 0.5
+    assert extrapolate([0.2, 0.1], [1.0, 2.0]) is None
+    assert [p.N for p in box_study("hcl", [8.0, 9.0, 10.0], 0.25)] == [32, 36, 40]
 
 
 def test_bo_gradient_composes_the_adjoint_terms(monkeypatch):

@@ -206,22 +206,24 @@ def test_helium_matches_oracle_and_virial():
     assert 0.8 < he.virial_ratio < 1.2
 
 
-@pytest.mark.parametrize("mode", ["energy", "box"])
-def test_grid_convergence_sweeps(mode, tmp_path):
+@pytest.mark.parametrize("study", ["spacing", "box"])
+def test_grid_convergence_sweeps(study, tmp_path):
     import json
 
     from gato_gb300.benchmarks.grid_convergence import main
     out_file = tmp_path / "conv.json"
-    if mode == "energy":
-        out = main(["--molecule", "water", "--mode", "energy", "--N", "24", "32", "40", "--L", "10",
-                    "--precision", "mixed", "--scf-iters", "60", "--json", str(out_file)])
+    if study == "spacing":
+        doc = main(["water", "spacing", "--N", "24", "32", "40", "--L", "10", "--precision", "mixed",
+                    "--max-scf", "60", "--out", str(out_file), "--quiet"])
+        fit = doc["summary"]["E_vs_h"]
     else:
-        out = main(["--molecule", "hcl", "--mode", "box", "--box-L", "8", "9", "10", "--target-h", "0.25",
-                    "--scf-iters", "60", "--json", str(out_file)])
-        assert out["h_drift"] is False and [r["N"] for r in out["rows"]] == [32, 36, 40]
-    assert all(r["converged"] for r in out["rows"])
-    assert out["fit"] is not None and math_isfinite(out["fit"]["extrapolated"])
-    assert json.loads(out_file.read_text())["rows"][0]["N"] == out["rows"][0]["N"]
+        doc = main(["hcl", "box", "--sides", "8", "9", "10", "--h", "0.25", "--precision", "fp64",
+                    "--max-scf", "60", "--out", str(out_file), "--quiet"])
+        assert doc["summary"]["h_spread"] == 0.0 and [r["N"] for r in doc["records"]] == [32, 36, 40]
+        fit = doc["summary"]["E_vs_inv_L"]
+    assert all(r["converged"] for r in doc["records"])
+    assert fit is not None and math_isfinite(fit["y_inf"])
+    assert json.loads(out_file.read_text())["records"][0]["N"] == doc["records"][0]["N"]
 
 
 def math_isfinite(x):
