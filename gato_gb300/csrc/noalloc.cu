@@ -1,28 +1,29 @@
 // gato_dot_noalloc: the grid inner product without any device allocation.
 //
-// Some callers cannot call cudaMalloc: code running while a stream is being
-// captured into a CUDA graph (allocation is not a capturable operation),
-// hosts that hand the GPU a fixed memory budget through their own allocator
-// and forbid the CUDA runtime's, and latency-critical threads that must not
-// block in the driver. gato_dot obtains its partial sums from per-stream
-// scratch that is allocated on first use; this variant keeps them in a
-// file-scope __device__ array instead. That array (kNoAllocChunks doubles,
-// 512 KiB) exists on every GPU that loads the library until the process
-// exits.
+// Some callers cannot call cudaMalloc: hosts that hand the GPU a fixed memory
+// budget through their own allocator and forbid the CUDA runtime's (an
+// embedding framework that owns every byte of device memory), and
+// latency-critical threads that must not block in the driver (cudaMalloc may
+// synchronise the device and takes driver locks). gato_dot obtains its
+// partial sums from per-stream scratch that is allocated on first use; this
+// variant keeps them in a file-scope __device__ array instead. That array
+// (kNoAllocChunks doubles, 512 KiB) exists on every GPU that loads the
+// library until the process exits.
 //
 // Set-up: the first call on each device, with that device current, looks up
 // the array's device address with cudaGetSymbolAddress (the host-side name of
-// a __device__ variable is only a stand-in, never a device pointer). Make
-// that first call before any stream capture. Every later call allocates
-// nothing.
+// a __device__ variable is only a stand-in, never a device pointer) and caches
+// it per device. Make that first call before any stream capture. Every later
+// call allocates nothing and takes no lock.
 //
 // Limits and sharing: one partial sum per 2048-element chunk, so n may not
 // exceed kNoAllocChunks * 2048 = 2^27 elements (a 512^3 grid); larger n is
-// rejected with GATO_EBADARG. All calls share the one array: calls whose
-// kernels overlap on the GPU (different streams, or different host threads
-// without ordering) race on it and must be serialised by the caller. Each
-// call overwrites every partial it reads, so nothing needs clearing between
-// calls.
+// rejected with GATO_EBADARG before any device work. All calls share the one
+// array: any two calls whose kernels can run at the same time on the GPU
+// (different streams, or different host threads without ordering) race on it
+// and must be serialised by the caller. Each call overwrites every partial it
+// reads, so nothing needs clearing between calls.
+#include <atomic>
 #include <map>
 #include <mutex>
 
@@ -38,21 +39,33 @@ constexpr int64_t kNoAllocChunk = (int64_t)kNoAllocThreads * kNoAllocEPT;   // 2
 
 __device__ __align__(256) double g_noalloc_partials[kNoAllocChunks];
 
+// device -> address of g_noalloc_partials: a lock-free slot per device id
+// below kNoAllocDevs (set once, read on every call), a locked map beyond.
+constexpr int kNoAllocDevs = 64;
+std::atomic<double*> g_noalloc_slot[kNoAllocDevs];
 std::mutex g_noalloc_mu;
-std::map<int, double*> g_noalloc_addr;   // device -> address of g_noalloc_partials
+std::map<int, double*> g_noalloc_addr;
 
 int noalloc_partials(double** out) {
   int dev = 0;
   GATO_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev >= 0 && dev < kNoAllocDevs) {
+    double* p = g_noalloc_slot[dev].load(std::memory_order_acquire);
+    if (p) {
+      *out = p;
+      return GATO_OK;
+    }
+  }
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
   auto it = g_noalloc_addr.find(dev);
-  if (it != g_noalloc_addr.end()) {
-    *out = it->second;
-    return GATO_OK;
-  }
   double* p = nullptr;
-  GATO_CUDA_TRY(cudaGetSymbolAddress((void**)&p, g_noalloc_partials));
-  g_noalloc_addr[dev] = p;
+  if (it != g_noalloc_addr.end()) {
+    p = it->second;
+  } else {
+    GATO_CUDA_TRY(cudaGetSymbolAddress((void**)&p, g_noalloc_partials));
+    g_noalloc_addr[dev] = p;
+  }
+  if (dev >= 0 && dev < kNoAllocDevs) g_noalloc_slot[dev].store(p, std::memory_order_release);
   *out = p;
   return GATO_OK;
 }

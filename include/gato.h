@@ -68,14 +68,15 @@ long long gato_launch_count(void);
  * The FP32 path accumulates products in float-float and blocks in FP64.   */
 int gato_dot(int dtype, const void* a, const void* b, int64_t n, double scale,
              double* out_dev, void* stream);
-/* gato_dot for callers that cannot allocate device memory (code running
- * during CUDA-graph stream capture, hosts that forbid the CUDA runtime's
- * allocator, latency-critical threads). No counterpart in the reference.
- * Its partial sums live in a library-owned static device array (512 KiB per
- * GPU, resident until exit) instead of lazily allocated scratch; the first
- * call on a device looks up that array's address, so make it before any
- * stream capture. n is limited to 2^27 elements (GATO_EBADARG beyond).
- * Calls share the array: calls that overlap on the GPU race.            */
+/* gato_dot for callers that cannot allocate device memory: hosts that own
+ * all device memory through their own allocator and forbid the CUDA
+ * runtime's, and latency-critical threads that must not block in cudaMalloc.
+ * No counterpart in the reference. Its partial sums live in a library-owned
+ * static device array (512 KiB per GPU, resident until exit) instead of
+ * lazily allocated scratch; the first call on a device looks up that array's
+ * address, so make it before any stream capture. n is limited to 2^27
+ * elements (GATO_EBADARG beyond). Calls share the array: any two calls whose
+ * kernels can run at the same time on the GPU race.                      */
 int gato_dot_noalloc(int dtype, const void* a, const void* b, int64_t n, double scale,
                      double* out_dev, void* stream);
 /* a[i] *= 1/sqrt(norm_dev[0]) -- the divide of grid.py:72-73.            */

@@ -1,12 +1,13 @@
 """gato_dot_noalloc: the grid inner product for callers that cannot allocate.
 
-Callers that run while a stream is captured into a CUDA graph, or that
-forbid the CUDA runtime's allocator, cannot use gato_dot (whose partial sums
+Hosts that own all device memory through their own allocator, and threads
+that must not block in cudaMalloc, cannot use gato_dot (whose partial sums
 come from scratch allocated on first use). gato_dot_noalloc keeps them in a
-static device array; this file checks it through the C ABI against gato_dot
-on two calls in a row (the array keeps the previous call's contents, which
-must not leak into the next result) and checks the size limit. It is named
-to be collected last, and passes alone in a fresh process or after the rest.
+static device array. This file calls it through the C ABI on two calls in a
+row (the array keeps the previous call's contents, which must not leak into
+the next result) and compares each result with gato_dot and with an FP64
+NumPy sum of the same inputs; it also checks the size limit. It is named to
+be collected last, and passes alone in a fresh process or after the rest.
 """
 import ctypes as C
 
@@ -41,12 +42,18 @@ def test_noalloc_dot_matches_dot_twice(lib, dtype):
     g2 = [torch.tensor(rng.standard_normal(24 ** 3 + 5), device="cuda", dtype=dtype) for _ in range(2)]
     tol = 1e-12 if dtype == torch.float64 else 1e-6
     for a, b in (g1, g2):
+        a64, b64 = a.double().cpu().numpy(), b.double().cpu().numpy()
+        exact = 0.125 * float(np.dot(a64, b64))
+        exact_sum = float(np.sum(a64))
         ref = _dot(lib, "gato_dot", a, b, 0.125)
         got = _dot(lib, "gato_dot_noalloc", a, b, 0.125)
         assert abs(got - ref) <= tol * max(1.0, abs(ref)), (got, ref)
+        # the FP32 path sums exact products in float-float: FP64-level agreement with numpy
+        assert abs(got - exact) <= 1e-12 * max(1.0, abs(exact)), (got, exact)
         ref_sum = _dot(lib, "gato_dot", a, None, 1.0)
         got_sum = _dot(lib, "gato_dot_noalloc", a, None, 1.0)
         assert abs(got_sum - ref_sum) <= tol * max(1.0, abs(ref_sum))
+        assert abs(got_sum - exact_sum) <= 1e-12 * max(1.0, abs(exact_sum)), (got_sum, exact_sum)
 
 
 def test_noalloc_dot_rejects_oversized_input(lib):
