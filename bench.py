@@ -811,7 +811,7 @@ def main():
     ap.add_argument("--profile", default=None, choices=["block", "matvec", "scf"],
                     help="run only the block / matvec Fock apply or two SCF iterations (for ncu captures)")
     ap.add_argument("--profile-dtype", default="f32", choices=["f32", "f64"])
-    ap.add_argument("--engine", type=int, default=0, choices=[0, 1, 2, 3],
+    ap.add_argument("--engine", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="FFT engine of the --profile run (see gato_poisson_tune)")
     args = ap.parse_args()
     if args.warmup < 3:

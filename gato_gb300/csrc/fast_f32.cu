@@ -1,7 +1,7 @@
 // Instantiations of the register-resident pair-solve kernels for float fields.
 // Table: M = 2N -> (R1, R2, lines per CTA); R1 is even so the zero-padded
 // half of every transform maps to whole register slots.
-#include "poisson_fast.cuh"
+#include "poisson_packed.cuh"
 
 namespace gato {
 namespace fast {
@@ -68,6 +68,26 @@ int rows_inv_j<T>(int M, const PassArgs& a, int f0, int nfg, const T2* S1, const
 #define X(MM, A, B, L32, L64) \
   case MM: return Launch<T, A, B, kF32 ? L32 : L64>::rows_inv_j(a, f0, nfg, S1, tw, s);
   switch (M) { GATO_FAST_SHAPES(X) }
+#undef X
+  return kNotHandled;
+}
+
+// Packed two-line column passes: M -> (R1, R2), 8 line pairs per CTA.
+#define GATO_PACKED_SHAPES(X) X(128, 8, 16) X(160, 10, 16) X(192, 12, 16) X(256, 16, 16) X(320, 20, 16)
+
+int packed_r2(int M) {
+#define X(MM, A, B) \
+  case MM: return B;
+  switch (M) { GATO_PACKED_SHAPES(X) }
+#undef X
+  return 0;
+}
+
+int packed_cols(int M, int mode, const float2* in, float2* out, const ColGeom& g, int outer, int nf,
+                const float4* tw4, const float* ghat2, int H, cudaStream_t s) {
+#define X(MM, A, B) \
+  case MM: return packed::LaunchP<A, B, 8>::cols(mode, in, out, g, outer, nf, tw4, ghat2, s);
+  switch (M) { GATO_PACKED_SHAPES(X) }
 #undef X
   return kNotHandled;
 }

@@ -91,6 +91,18 @@ __global__ void k_ghat_extract(const double2* X, T* ghat, int M, int H, double s
   }
 }
 
+// The packed FP32 engine's kernel spectrum: the octant unfolded along z,
+// ghat2[(kxo H + kyo) M + kz] = ghat[(kxo H + kyo) H + min(kz, M - kz)], so a
+// column pair (kz, kz + 1) reads one aligned float2.
+__global__ void k_ghat_unfold_z(const float* ghat, float* ghat2, int M, int H) {
+  const int64_t n = (int64_t)H * H * M;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int kz = (int)(i % M);
+    const int64_t ab = i / M;
+    ghat2[i] = ghat[ab * H + (kz <= M - kz ? kz : M - kz)];
+  }
+}
+
 // ---- batched strided-line transforms ------------------------------------------
 
 template <typename T2, int MODE>
@@ -297,6 +309,10 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
   T2* S1 = (T2*)pl.S1;
   T2* S2 = (T2*)pl.S2;
   const int Lf = pl.engine != 1 ? fast::rows_L<T>(M) : 0;   // register engine, 0: generic
+  // FP32 register engine: the column passes run packed (two lines per thread) where M has an
+  // instantiation, unless engine 4 asks for the scalar ones; the FP64 spectral energy pass never
+  // meets an FP32 plan
+  const bool packed = sizeof(T) == 4 && Lf > 0 && pl.tw4 && pl.engine != 4;
   const int Lr = pick_L<T2>(M, 0, sizeof(T) == 4 ? 16 : 8);
   const int Li = pick_L<T2>(M, (size_t)args.nout * N * sizeof(T), sizeof(T) == 4 ? 16 : 8);
   const size_t sm_r = fft_smem<T2>(M, Lr);
@@ -345,6 +361,15 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
       // register-resident two-pass engine
       // engine 0: multi-field z forward from two fields, 2: never, 3: from three
       GATO_TRY(fast::rows_fwd<T>(M, args, f0, nfg, S1, tw2, pl.engine == 2 ? 0 : (pl.engine == 3 ? 1 : 2), s));
+      if (packed) {
+        // FP32 column passes on the packed two-line engine (S2 in the split pair layout)
+        GATO_TRY(fast::packed_cols(M, COL_FWD, (const float2*)S1, (float2*)S2, gy, N, nfg,
+                                   (const float4*)pl.tw4, nullptr, pl.H, s));
+        GATO_TRY(fast::packed_cols(M, COL_FMI, (const float2*)S2, (float2*)S2, gx, M, nfg,
+                                   (const float4*)pl.tw4, (const float*)pl.ghat2, pl.H, s));
+        GATO_TRY(fast::packed_cols(M, COL_INV, (const float2*)S2, (float2*)S1, gyi, N, nfg,
+                                   (const float4*)pl.tw4, nullptr, pl.H, s));
+      } else {
       GATO_TRY(fast::cols<T>(M, COL_FWD, S1, S2, gy, N, nfg, tw2, nullptr, pl.H, s));
       if constexpr (sizeof(T) == 8) {
         if (fe) {
@@ -355,6 +380,7 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
       }
       GATO_TRY(fast::cols<T>(M, COL_FMI, S2, S2, gx, M, nfg, tw2, (const T*)pl.ghat, pl.H, s));
       GATO_TRY(fast::cols<T>(M, COL_INV, S2, S1, gyi, N, nfg, tw2, nullptr, pl.H, s));
+      }
       if (epi == EPI_J)
         GATO_TRY(fast::rows_inv_j<T>(M, args, f0, nfg, S1, tw2, s));
       else
@@ -446,6 +472,18 @@ static int plan_create(int dtype, int N, double h, double eps, int max_fields, P
     GATO_CUDA_TRY(cudaMemcpy(pl.tw2, dtype == GATO_F64 ? (void*)t64.data() : (void*)t32.data(), bytes,
                              cudaMemcpyHostToDevice));
   }
+  if (const int R2 = dtype == GATO_F32 ? fast::packed_r2(M) : 0) {
+    // packed stage twiddles: entry k1 R2 + n2 = (c, c, s, s), (c, s) = exp(-2 pi i n2 k1 / M)
+    const int R1 = M / R2;
+    std::vector<float4> t4((size_t)R1 * R2);
+    for (int k1 = 0; k1 < R1; ++k1)
+      for (int n2 = 0; n2 < R2; ++n2) {
+        const float c = (float)tw64[(size_t)n2 * k1].x, sn = (float)tw64[(size_t)n2 * k1].y;
+        t4[(size_t)k1 * R2 + n2] = make_float4(c, c, sn, sn);
+      }
+    GATO_CUDA_TRY(cudaMalloc(&pl.tw4, t4.size() * sizeof(float4)));
+    GATO_CUDA_TRY(cudaMemcpy(pl.tw4, t4.data(), t4.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  }
   double2* tw_d = nullptr;
   GATO_CUDA_TRY(cudaMalloc(&tw_d, (size_t)M * sizeof(double2)));
   GATO_CUDA_TRY(cudaMemcpy(tw_d, tw64.data(), (size_t)M * sizeof(double2), cudaMemcpyHostToDevice));
@@ -471,6 +509,12 @@ static int plan_create(int dtype, int N, double h, double eps, int max_fields, P
   else
     k_ghat_extract<float><<<grid_for(oct, 256), 256, 0, s>>>(X, (float*)pl.ghat, M, pl.H, scale);
   GATO_LAUNCH_TRY();
+  if (pl.tw4) {
+    const int64_t n2 = (int64_t)pl.H * pl.H * M;
+    GATO_CUDA_TRY(cudaMalloc(&pl.ghat2, n2 * sizeof(float)));
+    k_ghat_unfold_z<<<grid_for(n2, 256), 256, 0, s>>>((const float*)pl.ghat, (float*)pl.ghat2, M, pl.H);
+    GATO_LAUNCH_TRY();
+  }
   GATO_CUDA_TRY(cudaStreamSynchronize(s));
   cudaFree(X);
   cudaFree(tw_d);
@@ -488,7 +532,7 @@ static int plan_create(int dtype, int N, double h, double eps, int max_fields, P
 }
 
 static void plan_free(PoissonPlan& pl) {
-  free_after_pending({pl.ghat, pl.tw, pl.tw2, pl.S1, pl.S2, pl.partials});
+  free_after_pending({pl.ghat, pl.tw, pl.tw2, pl.tw4, pl.ghat2, pl.S1, pl.S2, pl.partials});
   pl = PoissonPlan{};
 }
 
@@ -595,6 +639,17 @@ extern "C" int gato_poisson_stage(gato_poisson_t plan, int stage, int nf, void* 
     using T2 = std::remove_pointer_t<decltype(S1)>;
     using T = std::remove_const_t<std::remove_pointer_t<decltype(ghat)>>;
     const int mode = stage == 1 ? COL_FWD : (stage == 2 ? COL_FMI : COL_INV);
+    if constexpr (sizeof(T) == 4) {
+      if (pl.engine != 1 && pl.engine != 4 && pl.tw4 && fast::rows_L<T>(M) > 0) {
+        ColGeom g1{nrows * M, (int64_t)N * M * M, (int64_t)N * M, (int64_t)M * M, M, M, M, N, M};
+        ColGeom g2{(int64_t)N * M * M, (int64_t)N * M * M, M, M, (int64_t)M * M, (int64_t)M * M, M, N, N};
+        ColGeom g3{(int64_t)N * M * M, nrows * M, (int64_t)M * M, (int64_t)N * M, M, M, M, M, N};
+        return fast::packed_cols(M, mode, stage == 1 ? (const float2*)S1 : (const float2*)S2,
+                                 stage == 3 ? (float2*)S1 : (float2*)S2, stage == 1 ? g1 : (stage == 2 ? g2 : g3),
+                                 stage == 2 ? M : N, nf, (const float4*)pl.tw4,
+                                 stage == 2 ? (const float*)pl.ghat2 : nullptr, pl.H, s);
+      }
+    }
     if (pl.engine != 1 && fast::rows_L<T>(M) > 0) {
       ColGeom g1{nrows * M, (int64_t)N * M * M, (int64_t)N * M, (int64_t)M * M, M, M, M, N, M};
       ColGeom g2{(int64_t)N * M * M, (int64_t)N * M * M, M, M, (int64_t)M * M, (int64_t)M * M, M, N, N};
@@ -624,9 +679,10 @@ extern "C" int gato_poisson_stage(gato_poisson_t plan, int stage, int nf, void* 
 // engine (0: register-resident two-pass kernels where M has one, with the
 // multi-field z forward for groups of two or more fields; 1: generic; 2: the
 // register kernels with one z-forward CTA per field; 3: the register kernels
-// with the multi-field z forward from three fields).
+// with the multi-field z forward from three fields; 4: as 0, with the scalar
+// FP32 column passes instead of the packed two-line ones).
 extern "C" int gato_poisson_tune(gato_poisson_t plan, int group, int engine) {
-  if (!plan || group < 0 || group > plan->p.max_fields || engine < 0 || engine > 3)
+  if (!plan || group < 0 || group > plan->p.max_fields || engine < 0 || engine > 4)
     return fail(GATO_EBADARG, "gato_poisson_tune: bad arguments");
   plan->p.group = group;
   plan->p.engine = engine;

@@ -45,12 +45,15 @@ struct PoissonPlan {
   void* tw = nullptr;      // M twiddles exp(-2 pi i k / M)
   void* tw2 = nullptr;     // register engine: tw2[k1 S + n2] = exp(-2 pi i n2 k1 / M), M = R1 R2,
                            // S = fft2::tw_row_stride
+  void* tw4 = nullptr;     // packed FP32 engine: tw4[k1 R2 + n2] = (c, c, s, s), (c, s) = exp(-2 pi i n2 k1 / M)
+  void* ghat2 = nullptr;   // packed FP32 engine: kernel spectrum folded in x and y only, [kxo][kyo][kz < M]
   void* S1 = nullptr;      // max_fields x N x N x M complex
   void* S2 = nullptr;      // max_fields x N x M x M complex
   double* partials = nullptr;
   int npart_cap = 0;
   int group = 0;           // fields per launch group (0: max_fields)
   int engine = 0;          // 0: register two-pass kernels where M allows, 1: generic Stockham
+                           // (2, 3: z-forward variants; 4: as 0 with the scalar column passes)
 };
 
 enum PoissonEpi { EPI_ACC = 0, EPI_ENERGY = 1, EPI_J = 2 };
@@ -95,6 +98,11 @@ template <typename T>
 int cols(int M, int mode, const typename Cplx<T>::type* in, typename Cplx<T>::type* out,
          const ColGeom& g, int outer, int nf, const typename Cplx<T>::type* tw, const T* ghat,
          int H, cudaStream_t s);
+// FP32 column passes on the packed two-line engine (poisson_packed.cuh): R2 of
+// M = R1 R2 when M has an instantiation, else 0.
+int packed_r2(int M);
+int packed_cols(int M, int mode, const float2* in, float2* out, const ColGeom& g, int outer, int nf,
+                const float4* tw4, const float* ghat2, int H, cudaStream_t s);
 // x forward of the y-transformed fields and the kernel-weighted spectral power
 // per CTA (the energy epilogue without the inverse passes).
 template <typename T>

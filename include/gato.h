@@ -151,7 +151,9 @@ int gato_poisson_stage(gato_poisson_t plan, int stage, int nf, void* stream);
  * M in {32,48,64,80,96,128,160,192,256,320}, with the multi-field z
  * forward for two or more fields; 1: generic Stockham; 2: the register
  * kernels with one z-forward CTA per field; 3: the multi-field z forward
- * from three fields).                                                    */
+ * from three fields; 4: as 0 with the scalar FP32 column passes instead of
+ * the packed two-line ones, which FP32 plans use for M in
+ * {128,160,192,256,320}).                                                */
 int gato_poisson_tune(gato_poisson_t plan, int group, int engine);
 
 /* ---- scf.py ----------------------------------------------------------------

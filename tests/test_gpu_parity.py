@@ -188,7 +188,9 @@ def test_register_engine_matches_generic(dtype, N):
     psi = rng.standard_normal(og.shape)
     ref = o.exchange_apply(psi, np.moveaxis(orbs, 0, -1), og)
     outs = []
-    for engine, group in [(0, 0), (1, 0), (0, 1)]:
+    # engine 0 runs the FP32 column passes packed (two lines per thread) where M has them; 4 the
+    # scalar ones; 1 the generic engine
+    for engine, group in [(0, 0), (1, 0), (0, 1), (4, 0)]:
         plan = PoissonPlan(N, og.h, og.h / 2, dtype, max_fields=2)
         _lib.call("gato_poisson_tune", plan.handle, group, engine)
         out = torch.zeros(og.shape, dtype=dtype, device="cuda")
