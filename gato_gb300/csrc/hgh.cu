@@ -6,10 +6,14 @@
 // The non-local projectors are Gaussians; each atom's projectors are
 // evaluated once per geometry on a box of radius cut_sigmas * max r_l around
 // it (the reference rebuilds full-grid fields on every apply). An apply is
-// three launches: box overlaps <p_q|psi>, the h-matrix contraction, and one
-// scatter-add per atom (atoms run in order, so overlapping boxes never race).
+// one launch of a thread-block cluster per vector: its CTAs split the box
+// points, reduce the overlaps <p_q|psi> through distributed shared memory,
+// form the h-matrix contraction and scatter-add each atom's projectors in
+// turn (a cluster barrier between atoms, so overlapping boxes never race).
 #include <cmath>
 #include <vector>
+
+#include <cooperative_groups.h>
 
 #include "hgh.cuh"
 
@@ -316,6 +320,94 @@ __global__ void k_nl_add(T* out, const T* __restrict__ vals, const double* coef,
   }
 }
 
+// The whole apply for one vector b in one cluster of kNlCluster CTAs (grid
+// (kNlCluster, nb)): each CTA takes every kNlCluster-th stretch of every box,
+// reduces its partial overlaps per projector in shared memory, and after a
+// cluster barrier every CTA sums the kNlCluster partials of each projector in
+// rank order through distributed shared memory (the same sums in every CTA),
+// forms coef[q] = sum_j h_ij ov[block + j] and adds sum_q coef[q] p_q to out
+// over its share of each atom's box, atom by atom with a cluster barrier in
+// between. ov and coef of the vector are also left in global memory.
+namespace cg = cooperative_groups;
+constexpr int kNlCluster = 8;          // CTAs per vector (the portable cluster size)
+constexpr int kNlClThreads = 512;
+constexpr int kNlClMaxQ = 64;          // projectors of all atoms
+struct NlAtomRange {
+  int q0[kMaxAtoms], nq[kMaxAtoms];
+};
+
+template <typename T>
+__global__ void __cluster_dims__(kNlCluster, 1, 1) __launch_bounds__(kNlClThreads)
+    k_nl_apply_cluster(const T* __restrict__ psi, T* out, const T* __restrict__ vals, const int* q_atom,
+                       const int64_t* q_off, const int* boxes, const int* q_block, const int* q_n,
+                       const int* q_i, const double* q_h, int nq, int K, NlAtomRange ar, int N, double dV,
+                       double* ov_out, double* coef_out) {
+  cg::cluster_group cl = cg::this_cluster();
+  __shared__ double wsum[kNlClMaxQ][kNlClThreads / 32];
+  __shared__ double part[kNlClMaxQ];
+  __shared__ double ovs[kNlClMaxQ];
+  __shared__ T cf[kNlClMaxQ];
+  const int rank = (int)cl.block_rank(), b = blockIdx.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int start = rank * blockDim.x + threadIdx.x, stride = kNlCluster * blockDim.x;
+  const T* ps = psi + (int64_t)b * N * N * N;
+  T* o = out + (int64_t)b * N * N * N;
+  for (int q = 0; q < nq; ++q) {
+    const int* bx = boxes + 6 * q_atom[q];
+    const int nz = bx[5], nyz = bx[4] * bx[5], npts = bx[3] * nyz;
+    const T* pv = vals + q_off[q];
+    Acc<T> acc;
+    for (int t = start; t < npts; t += stride) {
+      const int x = bx[0] + t / nyz, y = bx[1] + (t % nyz) / nz, z = bx[2] + t % nz;
+      acc.add_prod(pv[t], ps[((int64_t)x * N + y) * N + z]);
+    }
+    double v = acc.value();
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) wsum[q][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < nq) {
+    double v = 0.0;
+    for (int w = 0; w < nw; ++w) v += wsum[threadIdx.x][w];
+    part[threadIdx.x] = v;
+  }
+  cl.sync();   // every CTA's partial overlaps are in its shared memory
+  if (threadIdx.x < nq) {
+    double v = 0.0;
+    for (int r = 0; r < kNlCluster; ++r) v += cl.map_shared_rank(part, r)[threadIdx.x];
+    ovs[threadIdx.x] = v * dV;
+  }
+  cl.sync();   // the remote reads are done (no CTA leaves while another reads it); ovs is complete
+  if (threadIdx.x < nq) {
+    const int q = threadIdx.x, blk = q_block[q], n = q_n[q], i = q_i[q];
+    double c = 0.0;
+    for (int j = 0; j < n; ++j) c += q_h[9 * q + 3 * i + j] * ovs[blk + j];
+    cf[q] = (T)c;
+    if (rank == 0) {
+      ov_out[b * nq + q] = ovs[q];
+      coef_out[b * nq + q] = c;
+    }
+  }
+  __syncthreads();
+  bool first = true;
+  for (int a = 0; a < K; ++a) {
+    const int nqa = ar.nq[a];
+    if (nqa == 0) continue;
+    if (!first) cl.sync();   // the previous atom's adds are done: boxes of two atoms may overlap
+    first = false;
+    const int q0 = ar.q0[a];
+    const int* bx = boxes + 6 * a;
+    const int nz = bx[5], nyz = bx[4] * bx[5], npts = bx[3] * nyz;
+    for (int t = start; t < npts; t += stride) {
+      T v = (T)0;
+      for (int k = 0; k < nqa; ++k) v += cf[q0 + k] * vals[q_off[q0 + k] + t];
+      const int x = bx[0] + t / nyz, y = bx[1] + (t % nyz) / nz, z = bx[2] + t % nz;
+      o[((int64_t)x * N + y) * N + z] += v;
+    }
+  }
+}
+
 // energy = 2 * sum_b sum_q ov[b][q] coef[b][q]
 __global__ void k_nl_energy(const double* ov, const double* coef, int n, double* out) {
   __shared__ double sh[32];
@@ -415,6 +507,27 @@ int nl_overlaps(Nonlocal& nl, const void* psi, int nb, cudaStream_t s) {
 int nonlocal_apply(Nonlocal& nl, const void* psi, void* out, int nb, cudaStream_t s) {
   if (nl.nq == 0) return GATO_OK;
   if (nb > Nonlocal::kMaxVec) return fail(GATO_EBADARG, "nonlocal: at most %d vectors", Nonlocal::kMaxVec);
+  bool small_boxes = true;
+  for (int a = 0; a < nl.K; ++a) small_boxes = small_boxes && nl.box[a].npts < (int64_t)1 << 30;
+  if (nl.nq <= kNlClMaxQ && nl.K <= kMaxAtoms && small_boxes) {
+    // one cluster launch per apply
+    NlAtomRange ar{};
+    for (int a = 0; a < nl.K; ++a) {
+      ar.q0[a] = nl.atom_q0[a];
+      ar.nq[a] = nl.atom_nq[a];
+    }
+    dim3 g(kNlCluster, nb);
+    if (nl.dtype == GATO_F64)
+      k_nl_apply_cluster<double><<<g, kNlClThreads, 0, s>>>(
+          (const double*)psi, (double*)out, (const double*)nl.vals, nl.d_q_atom, nl.d_q_off, nl.d_box,
+          nl.d_q_block, nl.d_q_n, nl.d_q_i, nl.d_q_h, nl.nq, nl.K, ar, nl.N, nl.dV, nl.ov, nl.coef);
+    else
+      k_nl_apply_cluster<float><<<g, kNlClThreads, 0, s>>>(
+          (const float*)psi, (float*)out, (const float*)nl.vals, nl.d_q_atom, nl.d_q_off, nl.d_box,
+          nl.d_q_block, nl.d_q_n, nl.d_q_i, nl.d_q_h, nl.nq, nl.K, ar, nl.N, nl.dV, nl.ov, nl.coef);
+    GATO_LAUNCH_TRY();
+    return GATO_OK;
+  }
   GATO_TRY(nl_overlaps(nl, psi, nb, s));
   for (int a = 0; a < nl.K; ++a) {
     if (nl.atom_nq[a] == 0) continue;

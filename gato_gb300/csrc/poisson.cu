@@ -360,7 +360,7 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
     if (Lf > 0) {
       // register-resident two-pass engine
       // engine 0: multi-field z forward from two fields, 2: never, 3: from three
-      GATO_TRY(fast::rows_fwd<T>(M, args, f0, nfg, S1, tw2, pl.engine == 2 ? 0 : (pl.engine == 3 ? 1 : 2), s));
+      GATO_TRY(fast::rows_fwd<T>(M, args, f0, nfg, S1, tw2, pl.engine == 2 ? 0 : (pl.engine == 3 ? 1 : (pl.engine == 4 ? 3 : 2)), s));
       if (packed) {
         // FP32 column passes on the packed two-line engine (S2 in the split pair layout)
         GATO_TRY(fast::packed_cols(M, COL_FWD, (const float2*)S1, (float2*)S2, gy, N, nfg,
@@ -680,7 +680,8 @@ extern "C" int gato_poisson_stage(gato_poisson_t plan, int stage, int nf, void* 
 // multi-field z forward for groups of two or more fields; 1: generic; 2: the
 // register kernels with one z-forward CTA per field; 3: the register kernels
 // with the multi-field z forward from three fields; 4: as 0, with the scalar
-// FP32 column passes instead of the packed two-line ones).
+// FP32 column passes instead of the packed two-line ones and the z forward
+// staging once per CTA instead of persistent CTAs with double-buffered staging).
 extern "C" int gato_poisson_tune(gato_poisson_t plan, int group, int engine) {
   if (!plan || group < 0 || group > plan->p.max_fields || engine < 0 || engine > 4)
     return fail(GATO_EBADARG, "gato_poisson_tune: bad arguments");

@@ -404,6 +404,107 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
   }
 }
 
+// The bulk-staged z forward as a persistent kernel: each CTA walks row blocks
+// blockIdx.x, blockIdx.x + gridDim.x, ... with the staging buffer doubled, so
+// one elected thread issues the next block's row copies (1-D bulk copies on
+// that buffer's mbarrier) before the current block is transformed and the
+// copies land under the transforms. Same transforms and output as
+// k_rows_fwd_multi. The host guarantees 16-byte aligned rows, a padded staged
+// row that is a multiple of 16 bytes and L | N^2; the kernel re-checks the
+// alignment and records error 110 instead of issuing a bad copy. Waits are
+// bounded (codes 113/114).
+template <typename T, int R1, int R2, int L>
+__global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
+    k_rows_fwd_pers(PassArgs args, RowsIn ri, int f0, int nfg, typename Cplx<T>::type* S1,
+                    const typename Cplx<T>::type* tw, int* err) {
+  using T2 = typename Cplx<T>::type;
+  constexpr int M = R1 * R2, N = M / 2, NP = StageRow<R1, R2>::NP, RM = Shape<R1, R2>::RMAX, NT = L * RM;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ __align__(8) uint64_t sbar[2];
+  __shared__ int s_misaligned;
+  T2* buf = reinterpret_cast<T2*>(smraw);
+  T2* tws = buf + L * RowBuf<R1, R2>::LS;
+  T* stage0 = reinterpret_cast<T*>(tws + R1 * TwRow<T2, R2>::S);   // [slot][input][line][z], rows of NP
+  const int SB = ri.nin * L * NP;                                    // floats per staging slot
+  const int64_t nrows = (int64_t)N * N;
+  const int nblk = (int)(nrows / L);
+  if (threadIdx.x == 0) {
+    mbar_init(&sbar[0], 1);
+    mbar_init(&sbar[1], 1);
+    fence_barrier_init();
+    int bad_align = (int)((smem_u32(stage0) | (uint32_t)(SB * sizeof(T)) | (uint32_t)(NP * sizeof(T)) |
+                           (uint32_t)(N * sizeof(T))) & 15u);
+    for (int sl = 0; sl < ri.nin; ++sl)
+      bad_align |= (int)(reinterpret_cast<uintptr_t>(args.in[ri.idx[sl]]) & 15u);
+    s_misaligned = bad_align;
+    if (bad_align && err) atomicExch(err, 110);
+  }
+  for (int i = threadIdx.x; i < R1 * TwRow<T2, R2>::S; i += NT) tws[i] = tw[i];
+  __syncthreads();
+  if (s_misaligned) return;
+  auto issue = [&](int blk, int slot) {
+    mbar_expect_tx(&sbar[slot], (uint32_t)(ri.nin * L * N * sizeof(T)));
+    T* st = stage0 + slot * SB;
+    for (int sl = 0; sl < ri.nin; ++sl) {
+      const T* src = reinterpret_cast<const T*>(args.in[ri.idx[sl]]) + (int64_t)blk * L * N;
+      for (int l = 0; l < L; ++l)
+        bulk_load(st + (sl * L + l) * NP, src + (int64_t)l * N, (uint32_t)(N * sizeof(T)), &sbar[slot]);
+    }
+  };
+  if (threadIdx.x == 0 && (int)blockIdx.x < nblk) issue(blockIdx.x, 0);
+  const int line = threadIdx.x / RM, j = threadIdx.x % RM;
+  int it = 0;
+  for (int blk = blockIdx.x; blk < nblk; blk += gridDim.x, ++it) {
+    const int slot = it & 1;
+    // the other slot was last read by the previous block, which ended at a barrier
+    const bool more = blk + (int)gridDim.x < nblk;
+    if (threadIdx.x == 0 && more) issue(blk + gridDim.x, slot ^ 1);
+    const bool bad = !mbar_wait_bounded(&sbar[slot], (it >> 1) & 1, err, 113);
+    if (__syncthreads_or(bad)) {
+      if (threadIdx.x == 0) {   // copies still in flight land before the CTA goes away
+        mbar_wait_bounded(&sbar[slot], (it >> 1) & 1, err, 114);
+        if (more) mbar_wait_bounded(&sbar[slot ^ 1], ((it + 1) >> 1) & 1, err, 114);
+      }
+      return;
+    }
+    const T* stage = stage0 + slot * SB;
+    const int64_t r = (int64_t)blk * L + line;
+    for (int p = 0; p < nfg; ++p) {
+      const FieldDesc& fd = args.f[f0 + p];
+      if (j < R2) {
+        const int a0 = ri.slot_of[fd.p[0].a];
+        const int b0 = fd.p[0].b >= 0 ? ri.slot_of[fd.p[0].b] : -1;
+        const int a1 = fd.p[1].a >= 0 ? ri.slot_of[fd.p[1].a] : -1;
+        const int b1 = (a1 >= 0 && fd.p[1].b >= 0) ? ri.slot_of[fd.p[1].b] : -1;
+        T2 v[R1];
+#pragma unroll
+        for (int n1 = 0; n1 < R1 / 2; ++n1) {
+          const int z = R2 * n1 + j;
+          T x = stage[(a0 * L + line) * NP + z];
+          if (b0 >= 0) x *= stage[(b0 * L + line) * NP + z];
+          T y = (T)0;
+          if (a1 >= 0) {
+            y = stage[(a1 * L + line) * NP + z];
+            if (b1 >= 0) y *= stage[(b1 * L + line) * NP + z];
+          }
+          v[n1].x = x;
+          v[n1].y = y;
+        }
+        row_fwd_stage1<T2, R1, R2, true>(buf, line, j, v);
+      }
+      __syncthreads();
+      if (j < R1) {
+        T2 X[R2];
+        row_fwd_stage2<T2, R1, R2>(buf, line, j, tws, X);
+        T2* d = S1 + (int64_t)p * nrows * M + r * M + j;
+#pragma unroll
+        for (int k2 = 0; k2 < R2; ++k2) d[R1 * k2] = X[k2];
+      }
+      __syncthreads();   // buf is rewritten by the next field; the stage slot is free after the last
+    }
+  }
+}
+
 // z inverse over every field of the group, then the epilogue. NO > 0: the
 // accumulation terms target outputs < NO, kept in registers (each thread owns
 // the R1/2 fixed elements z = j + R2 n1 of its row); NO == 0: energy mode.
@@ -625,6 +726,8 @@ struct Launch {
     return GATO_OK;
   }
   // multi: 0 per-field CTAs, 1 multi-field CTAs from three fields up, 2 from two fields up
+  // (persistent, double-buffered staging where the rows allow bulk copies), 3 as 2 with one
+  // staging round trip per CTA (the non-persistent kernel)
   // (the default: with bulk staging the multi-field kernel wins at two fields too,
   // 239 against 244 us for the 128^3 matvec)
   static int rows_fwd(const PassArgs& a, int f0, int nfg, T2* S1, const T2* tw, int multi, cudaStream_t s) {
@@ -647,7 +750,7 @@ struct Launch {
     // field at once, so smaller CTAs give more of them and a shorter last wave
     constexpr int LM = L >= 16 ? L / 2 : L;
     const size_t stage_bytes = (size_t)ri.nin * LM * StageRow<R1, R2>::NP * sizeof(T);
-    if (multi > 0 && nfg >= (multi == 2 ? 2 : 3) && stage_bytes <= 48 * 1024) {
+    if (multi > 0 && nfg >= (multi == 1 ? 3 : 2) && stage_bytes <= 48 * 1024) {
       const size_t sm = (size_t)(LM * RowBuf<R1, R2>::LS + TWN) * sizeof(T2) + stage_bytes;
       const int64_t nrows = (int64_t)N * N;
       // a bulk copy needs 16-byte aligned source and destination rows and a
@@ -656,7 +759,23 @@ struct Launch {
                   (StageRow<R1, R2>::NP * sizeof(T)) % 16 == 0;
       for (int i = 0; i < ri.nin; ++i) bulk = bulk && ((uintptr_t)a.in[ri.idx[i]] % 16) == 0;
       const unsigned grid = (unsigned)((nrows + LM - 1) / LM);
-      if (bulk) {
+      if (bulk && multi != 3) {
+        // persistent CTAs over the row blocks, double-buffered staging: one resident wave
+        auto kern = k_rows_fwd_pers<T, R1, R2, LM>;
+        const size_t smp = sm + stage_bytes;   // a second staging slot
+        GATO_TRY(smem_attr(kern, smp));
+        static int per_sm[kMaxIn + 1] = {}, sms = 0;   // resident CTAs per SM by staged inputs
+        int& ps = per_sm[ri.nin];
+        if (ps == 0) {
+          int dev = 0;
+          GATO_CUDA_TRY(cudaGetDevice(&dev));
+          GATO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+          GATO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, kern, LM * Shape<R1, R2>::RMAX, smp));
+          if (ps < 1) return fail(GATO_EUNSUPPORTED, "z forward: no resident CTA fits");
+        }
+        const unsigned pg = (unsigned)std::min<int64_t>(grid, (int64_t)ps * sms);
+        kern<<<pg, LM * Shape<R1, R2>::RMAX, smp, s>>>(a, ri, f0, nfg, S1, tw, device_error_word());
+      } else if (bulk) {
         GATO_TRY(smem_attr(k_rows_fwd_multi<T, R1, R2, LM, true>, sm));
         k_rows_fwd_multi<T, R1, R2, LM, true><<<grid, LM * Shape<R1, R2>::RMAX, sm, s>>>(
             a, ri, f0, nfg, S1, tw, device_error_word());

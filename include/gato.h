@@ -153,7 +153,8 @@ int gato_poisson_stage(gato_poisson_t plan, int stage, int nf, void* stream);
  * kernels with one z-forward CTA per field; 3: the multi-field z forward
  * from three fields; 4: as 0 with the scalar FP32 column passes instead of
  * the packed two-line ones, which FP32 plans use for M in
- * {128,160,192,256,320}).                                                */
+ * {128,160,192,256,320}, and a z forward that stages once per CTA
+ * instead of persistent CTAs with double-buffered staging).              */
 int gato_poisson_tune(gato_poisson_t plan, int group, int engine);
 
 /* ---- scf.py ----------------------------------------------------------------
