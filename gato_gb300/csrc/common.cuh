@@ -43,7 +43,7 @@ int* device_error_word();
 // The first call on a stream may allocate; later calls of the same or
 // smaller size do not. Slot 0 serves leaf reductions; a driver that calls
 // leaf operations while holding scratch uses its own slot.
-enum ScratchSlot { kSlotLeaf = 0, kSlotLanczos = 1, kSlotImagTime = 2, kSlotCount = 3 };
+enum ScratchSlot { kSlotLeaf = 0, kSlotLanczos = 1, kSlotImagTime = 2, kSlotLanczosSweep = 3, kSlotCount = 4 };
 void* stream_scratch(cudaStream_t s, size_t bytes, int slot = kSlotLeaf);
 // Free every scratch slot of stream s (synchronises s first): for private
 // streams that are about to be destroyed.

@@ -24,6 +24,8 @@
 #include <cmath>
 #include <type_traits>
 
+#include <cuda.h>
+
 #include "op.cuh"
 #include "ptx.cuh"
 
@@ -1061,12 +1063,463 @@ int lz_finish(const T* Vb, int64_t n, int m, int K, double tol, const double* al
   return GATO_OK;
 }
 
+// ---- one basis sweep per step (FP32 basis) ------------------------------------------
+// The classical Gram-Schmidt step above reads the basis twice: once for the
+// coefficients c = V^T w'' and once for the correction w'' - V c. Here the
+// operator is applied to the uncorrected three-term vector
+//   w^_j = F v_j - beta_{j-1} v_{j-1} - alpha_j v_j,
+// and the sweep of step j+1 recovers both the new basis vector and its image,
+//   v_{j+1}   = (w^_j - V_j c_j) / beta_j,
+//   F v_{j+1} = (F w^_j - F V_j c_j) / beta_j,  F V_j c_j = V_{j+1} g,  g = T~ c_j,
+// from the Lanczos relation F v_k = beta_{k-1} v_{k-1} + alpha_k v_k + beta_k v_{k+1}
+// + V_k c_k, which holds for the computed quantities to rounding (T~ is the
+// upper Hessenberg matrix of alpha, beta and every earlier c). The same sweep
+// forms the projections of the next step from the identity
+//   c_{j+1,k} = <v_k, F v_{j+1}> - beta_j <v_k, v_j> - alpha_{j+1} <v_k, v_{j+1}>,
+// taking <v_k, v_j> from the previous sweep. So each step reads the basis once
+// (plus four vectors), where the two-sweep form reads it twice; in exact
+// arithmetic both give the reference's v, alpha and beta. beta_j comes from
+// |w^_j|^2 - |c_j|^2 (Pythagoras; the c_j are the small reorthogonalisation
+// coefficients), |w^_j|^2 summed in float-float when w^_j is formed.
+//
+// Sweep kernel: persistent blocks walk chunks of 64-256 elements; a producer
+// warp stages rows v_0..v_{j-1} of a chunk (one 2-D TMA box), w^ and F w^ (two
+// 1-D bulk copies) into a ring of shared buffers (full/empty mbarriers,
+// bounded waits); the consumers form v_j and F v_j of the chunk (256 / width
+// threads per element, each over a share of the basis), write them out and
+// keep them as two more rows, and 1-8 threads per basis vector k accumulate
+// <v_k, F v_j> and <v_k, v_j> over their chunks (FP32 per chunk, FP64 across
+// chunks). Chunk width, ring depth and blocks per SM follow j (fz_ce,
+// fz_stages). Only the FP32 basis takes this path: FP64 products would make
+// the sweep FP64-bound on GB300.
+constexpr int kFzCE = 128;                  // the middle chunk width; n must be a multiple
+constexpr int kFzWarps = 8;                 // consumer warps
+constexpr int kFzThreads = 32 * (kFzWarps + 1);
+constexpr int kFzMaxM = 200;                // basis rows + 4 of a chunk, two buffers, fit in shared memory
+
+__device__ __forceinline__ void named_sync(int id, int n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+// Named barrier over n threads that also ORs a predicate: every participant gets the same answer.
+__device__ __forceinline__ bool named_sync_or(int id, int n, bool v) {
+  int r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.s32 q, %3, 0;\n\tbar.red.or.pred p, %1, %2, q;\n\t"
+      "selp.s32 %0, 1, 0, p;\n\t}"
+      : "=r"(r)
+      : "r"(id), "r"(n), "r"((int)v)
+      : "memory");
+  return r != 0;
+}
+
+// Chunk width of a step-j sweep: 256 elements while the basis is short (fewer, larger chunks
+// amortise the per-chunk latency), 128 while two blocks' staging fits one SM (j <= 98), then 64
+// (measured at 128^3: 64-wide chunks lose to 128 below j = 100 and win above). The element count
+// must divide into chunks (n % 256 == 0 for the widest).
+__host__ __device__ constexpr int fz_ce(int j, int64_t n) {
+  return (j < 32 && n % 256 == 0) ? 256 : (j < 99 ? 128 : 64);
+}
+// Threads per projection row in phase B: as many as keep (j + 1) rows within the 256 consumers.
+__host__ __device__ constexpr int fz_tpk(int j) { return j < 32 ? 8 : (j < 64 ? 4 : (j < 128 ? 2 : 1)); }
+// Staged row width (floats): the chunk plus a pad that makes the 16-byte reads of one phase-B
+// phase (8 threads: 8 / tpk rows, tpk consecutive vectors each) fall in 8 distinct 4-bank groups:
+// the row stride is 4 tpk words mod 32. The staging copy's box is this wide (the extra columns are
+// the next chunk's, or zero past the end of the vector).
+__host__ __device__ constexpr int fz_rw(int j, int ce) { return fz_tpk(j) == 8 ? ce : ce + 4 * fz_tpk(j); }
+// floats per staging buffer: j + 4 rows, rounded up to 128 bytes (TMA destinations)
+__host__ __device__ constexpr int fz_bufstride(int j, int ce) {
+  return ((j + 4) * fz_rw(j, ce) * 4 + 127) / 128 * 32;
+}
+
+constexpr int kFzMaxStages = 32;   // small-j chunks are a few KB: many in flight per SM
+constexpr size_t kFzFixed = 2 * (kFzMaxM + 2) * sizeof(float) + 4 * kFzCE * sizeof(float) +
+                            2 * kFzMaxStages * sizeof(uint64_t) + 128;
+constexpr size_t kFzSmemCap = 220 * 1024;
+__host__ __device__ constexpr size_t fz_smem(int j, int ce, int nst) {
+  return (size_t)nst * fz_bufstride(j, ce) * sizeof(float) + kFzFixed;
+}
+// Staging depth of a step-j sweep: as many buffers as let two blocks share an SM (the two blocks
+// hide each other's per-chunk latency), else as many as one block can hold (at least two).
+inline int fz_stages(int j, int ce) {
+  const size_t half = 113 * 1024 - kFzFixed;   // two blocks and their reserved shared memory per SM
+  const int n2 = (int)(half / (fz_bufstride(j, ce) * sizeof(float)));
+  if (n2 >= 2) return n2 < kFzMaxStages ? n2 : kFzMaxStages;
+  const int nst = (int)((kFzSmemCap - kFzFixed) / (fz_bufstride(j, ce) * sizeof(float)));
+  return nst < kFzMaxStages ? nst : kFzMaxStages;
+}
+
+// j: this sweep forms v_j (basis slot j) and u_j = F v_j (U). wh: w^_{j-1}; z: F w^_{j-1};
+// c (j entries), g (j + 1 entries), binv = {beta_{j-1}, 1 / beta_{j-1}}. part: [2][j+1][grid].
+// tv: the basis as a 2-D tensor {n, slots} with a {fz_rw(j), j} box: one copy stages rows
+// v_0..v_{j-1} of a chunk in the padded row layout the sweep reads.
+// At most 96 registers, so two blocks (18 warps) fit one SM's register file.
+__global__ void __maxnreg__(96)
+    k_fz_sweep(const __grid_constant__ CUtensorMap tv, float* V, int64_t n, int j, int CE, int NST, const float* wh,
+               const float* z, float* U, const double* c, const double* g, const double* binv, double* part,
+               int* err) {
+  extern __shared__ __align__(128) unsigned char fzs[];
+  unsigned char* base = fzs + ((128u - (smem_u32(fzs) & 127u)) & 127u);
+  float* buf0 = reinterpret_cast<float*>(base);
+  const int BS = fz_bufstride(j, CE), RW = fz_rw(j, CE), TPK = fz_tpk(j);   // NST staging buffers
+  float* cs = buf0 + (size_t)NST * BS;
+  float* gs = cs + (kFzMaxM + 2);
+  float* pa = gs + (kFzMaxM + 2);                // [2][P-1][CE]: the other groups' partial corrections
+  uint64_t* full = reinterpret_cast<uint64_t*>(pa + 4 * kFzCE);   // pa holds up to 2 x 3 x 64 floats
+  uint64_t* empty = full + kFzMaxStages;
+  __shared__ int abort_flag;
+  volatile int* abort_v = &abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t nch = n / CE;
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < NST; ++b) {
+      mbar_init(&full[b], 1);
+      mbar_init(&empty[b], kFzWarps);
+    }
+    abort_flag = 0;
+    fence_barrier_init();
+  }
+  for (int k = threadIdx.x; k < j; k += blockDim.x) cs[k] = (float)c[k];
+  for (int k = threadIdx.x; k <= j; k += blockDim.x) gs[k] = (float)g[k];
+  __syncthreads();
+  if (warp == kFzWarps) {   // producer
+    if (lane == 0) {
+      int it = 0;
+      for (int64_t ch = blockIdx.x; ch < nch; ch += gridDim.x, ++it) {
+        const int b = it % NST;
+        if (it >= NST && !mbar_wait_bounded(&empty[b], (uint32_t)(((it / NST) - 1) & 1), err, 115)) {
+          *abort_v = 1;
+          break;
+        }
+        if (*abort_v) break;
+        float* bf = buf0 + (size_t)b * BS;
+        const int64_t off = ch * CE;
+        const uint32_t RB = (uint32_t)CE * sizeof(float);
+        mbar_expect_tx(&full[b], (uint32_t)j * RW * sizeof(float) + 2 * RB);
+        if (j > 0) tma_load_2d(bf, &tv, &full[b], (int)off, 0);
+        bulk_load(bf + (size_t)(j + 2) * RW, wh + off, RB, &full[b]);
+        bulk_load(bf + (size_t)(j + 3) * RW, z + off, RB, &full[b]);
+      }
+      if (*abort_v)   // copies in flight land (bounded) before the block exits
+        for (int p = it > NST ? it - NST : 0; p < it; ++p)
+          mbar_wait_bounded(&full[p % NST], (uint32_t)((p / NST) & 1), err, 116);
+    }
+    return;
+  }
+  // consumers
+  const int t = threadIdx.x;
+  // phase A: element e of the chunk, group h of P = 256 / CE splitting the basis rows
+  const int P = 256 / CE;
+  const int e = t % CE, h = t / CE;
+  const int k0 = (int)((int64_t)j * h / P), k1 = (int)((int64_t)j * (h + 1) / P);
+  const int kb = t / TPK, sub = t % TPK;       // phase B: projection row kb, part sub of the chunk
+  const float bi = (float)binv[1];
+  const float gj = gs[j];
+  double accA = 0.0, accD = 0.0;
+  int it = 0;
+  bool ok = true;
+  for (int64_t ch = blockIdx.x; ch < nch; ch += gridDim.x, ++it) {
+    const int b = it % NST;
+    // one decision for every consumer: the producer may raise the flag at any moment
+    bool bad = *abort_v != 0;
+    if (!bad) bad = !mbar_wait_bounded(&full[b], (uint32_t)((it / NST) & 1), err, 117);
+    if (named_sync_or(1, kFzWarps * 32, bad)) {
+      if (t == 0) {
+        *abort_v = 1;   // the producer stops issuing
+        // this chunk's copies land (bounded) before the block can leave
+        mbar_wait_bounded(&full[b], (uint32_t)((it / NST) & 1), err, 118);
+      }
+      ok = false;
+      break;
+    }
+    float* bf = buf0 + (size_t)b * BS;
+    // phase A: corrections of this half of the basis, two accumulator pairs
+    float cv0 = 0.f, cu0 = 0.f, cv1 = 0.f, cu1 = 0.f;
+    int k = k0;
+    for (; k + 1 < k1; k += 2) {
+      const float x0 = bf[(size_t)k * RW + e], x1 = bf[(size_t)(k + 1) * RW + e];
+      cv0 = fmaf(cs[k], x0, cv0);
+      cu0 = fmaf(gs[k], x0, cu0);
+      cv1 = fmaf(cs[k + 1], x1, cv1);
+      cu1 = fmaf(gs[k + 1], x1, cu1);
+    }
+    if (k < k1) {
+      const float x0 = bf[(size_t)k * RW + e];
+      cv0 = fmaf(cs[k], x0, cv0);
+      cu0 = fmaf(gs[k], x0, cu0);
+    }
+    float cv = cv0 + cv1, cu = cu0 + cu1;
+    if (h > 0) {
+      pa[(h - 1) * CE + e] = cv;
+      pa[(P - 1 + h - 1) * CE + e] = cu;
+    }
+    named_sync(1, kFzWarps * 32);
+    const int64_t gi = ch * CE + e;
+    if (h == 0) {
+      for (int q = 1; q < P; ++q) {   // groups in order
+        cv += pa[(q - 1) * CE + e];
+        cu += pa[(P - 1 + q - 1) * CE + e];
+      }
+      const float vj = (bf[(size_t)(j + 2) * RW + e] - cv) * bi;
+      const float uj = (bf[(size_t)(j + 3) * RW + e] - cu - gj * vj) * bi;
+      bf[(size_t)j * RW + e] = vj;
+      bf[(size_t)(j + 1) * RW + e] = uj;
+      V[(int64_t)j * n + gi] = vj;
+      U[gi] = uj;
+    }
+    named_sync(1, kFzWarps * 32);
+    // phase B: the TPK threads of row kb <= j accumulate <v_kb, u_j> and <v_kb, v_j> over the
+    // chunk's 16-byte vectors sub, sub + TPK, ..., then reduce across those lanes
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), d = a;
+    if (kb <= j) {
+      const float4* rk = reinterpret_cast<const float4*>(bf + (size_t)kb * RW);
+      const float4* ru = reinterpret_cast<const float4*>(bf + (size_t)(j + 1) * RW);
+      const float4* rv = reinterpret_cast<const float4*>(bf + (size_t)j * RW);
+#pragma unroll 4
+      for (int i = sub; i < CE / 4; i += TPK) {
+        const float4 x = rk[i], u = ru[i], v = rv[i];
+        a.x = fmaf(x.x, u.x, a.x);
+        a.y = fmaf(x.y, u.y, a.y);
+        a.z = fmaf(x.z, u.z, a.z);
+        a.w = fmaf(x.w, u.w, a.w);
+        d.x = fmaf(x.x, v.x, d.x);
+        d.y = fmaf(x.y, v.y, d.y);
+        d.z = fmaf(x.z, v.z, d.z);
+        d.w = fmaf(x.w, v.w, d.w);
+      }
+    }
+    float sa = (a.x + a.y) + (a.z + a.w), sd = (d.x + d.y) + (d.z + d.w);
+    for (int o = TPK / 2; o > 0; o >>= 1) {   // TPK consecutive lanes of one warp
+      sa += __shfl_xor_sync(0xffffffffu, sa, o);
+      sd += __shfl_xor_sync(0xffffffffu, sd, o);
+    }
+    if (kb <= j && sub == 0) {
+      accA += (double)sa;
+      accD += (double)sd;
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[b]);
+  }
+  if (ok && kb <= j && sub == 0) {
+    const int G = gridDim.x;
+    part[(int64_t)kb * G + blockIdx.x] = accA;
+    part[(int64_t)(j + 1 + kb) * G + blockIdx.x] = accD;
+  }
+}
+
+// alpha_j and c_j from the sweep's partials (one block): a_k, d_k = dV * sums;
+// b_k = <v_k, v_{j-1}> from the previous sweep (k < j) and d_{j-1} (k = j);
+// alpha_j = a_j - beta_{j-1} b_j; c_k = a_k - beta_{j-1} b_k - alpha_j d_k.
+// Cm row j = c_j; dprev <- d.
+__global__ void k_fz_post1(const double* part, int G, int j, double dV, double* alphas, const double* betas,
+                           double* dprev, double* Cm, int m) {
+  __shared__ double sa[kFzMaxM + 1], sd[kFzMaxM + 1];
+  __shared__ double s_alpha;
+  // one warp per (k, dot): lanes read the block partials in parallel, then a fixed-order tree
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int r = warp; r < 2 * (j + 1); r += nw) {
+    double v = 0.0;
+    for (int q = lane; q < G; q += 32) v += part[(int64_t)r * G + q];
+    v = warp_sum(v);
+    if (lane == 0) {
+      if (r <= j) sa[r] = v * dV;
+      else sd[r - (j + 1)] = v * dV;
+    }
+  }
+  __syncthreads();
+  const double beta = j > 0 ? betas[j - 1] : 0.0;
+  if (threadIdx.x == 0) {
+    const double bj = j > 0 ? sd[j - 1] : 0.0;
+    s_alpha = sa[j] - beta * bj;
+    alphas[j] = s_alpha;
+  }
+  __syncthreads();
+  const double al = s_alpha;
+  for (int k = threadIdx.x; k <= j; k += blockDim.x) {
+    const double bk = j == 0 ? 0.0 : (k < j ? dprev[k] : sd[j - 1]);
+    Cm[(int64_t)j * m + k] = sa[k] - beta * bk - al * sd[k];
+  }
+  __syncthreads();   // every dprev read is done
+  for (int k = threadIdx.x; k <= j; k += blockDim.x) dprev[k] = sd[k];
+}
+
+// w^_j = u_j - beta_{j-1} v_{j-1} - alpha_j v_j (field type products) and its float-float |.|^2 partials.
+__global__ void k_fz_form(const float* __restrict__ U, const float* __restrict__ vm1, const float* __restrict__ vj,
+                          float* wh, int64_t n, const double* betas, const double* alphas, int j, double* part) {
+  __shared__ double sh[32];
+  const float be = j > 0 ? (float)betas[j - 1] : 0.f, al = (float)alphas[j];
+  Acc<float> acc;
+  const int64_t nv = n / 4;
+  const float4* U4 = reinterpret_cast<const float4*>(U);
+  const float4* A4 = reinterpret_cast<const float4*>(j > 0 ? vm1 : vj);
+  const float4* B4 = reinterpret_cast<const float4*>(vj);
+  float4* W4 = reinterpret_cast<float4*>(wh);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 u = U4[i], a = A4[i], b = B4[i];
+    float4 w;
+    w.x = u.x - be * a.x - al * b.x;
+    w.y = u.y - be * a.y - al * b.y;
+    w.z = u.z - be * a.z - al * b.z;
+    w.w = u.w - be * a.w - al * b.w;
+    W4[i] = w;
+    acc.add_prod(w.x, w.x);
+    acc.add_prod(w.y, w.y);
+    acc.add_prod(w.z, w.z);
+    acc.add_prod(w.w, w.w);
+  }
+  const double v = block_sum(acc.value(), sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = v;
+}
+
+// beta_j = sqrt(dV |w^_j|^2 - |c_j|^2), binv = {beta_j, 1 / beta_j or 0}, and the next sweep's
+// c = c_j and g_i = sum_k T~_{ik} c_k, i <= j + 1 (one block).
+__global__ void k_fz_post2(const double* part, int nb, double dV, const double* Cm, int m, int j,
+                           const double* alphas, double* betas, double* binv, double* c_next, double* g_next) {
+  __shared__ double sh[32];
+  __shared__ double sc[kFzMaxM + 1];
+  double v = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) v += part[i];
+  const double wn = block_sum(v, sh);   // valid in thread 0
+  double c2 = 0.0;
+  for (int k = threadIdx.x; k <= j; k += blockDim.x) {
+    const double ck = Cm[(int64_t)j * m + k];
+    sc[k] = ck;
+    c_next[k] = ck;
+    c2 += ck * ck;
+  }
+  __syncthreads();
+  const double cn = block_sum(c2, sh);
+  if (threadIdx.x == 0) {
+    const double b2 = wn * dV - cn;
+    const double beta = b2 > 0.0 ? sqrt(b2) : 0.0;
+    betas[j] = beta;
+    binv[0] = beta;
+    binv[1] = beta > 0.0 ? 1.0 / beta : 0.0;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i <= j + 1; i += blockDim.x) {
+    double gi = 0.0;
+    if (i + 1 <= j) gi += sc[i + 1] * betas[i];
+    if (i <= j) gi += sc[i] * alphas[i];
+    if (i >= 1) gi += sc[i - 1] * betas[i - 1];
+    for (int k = i; k <= j; ++k) gi += sc[k] * Cm[(int64_t)k * m + i];
+    g_next[i] = gi;
+  }
+}
+
+struct FzScratch {
+  float *wh, *z, *u;
+  double *Cm, *dprev, *c, *g, *binv, *part, *partn;
+  int grid, nbf, sms;   // grid: the most sweep blocks of any step
+};
+
+int fz_scratch(cudaStream_t s, int64_t n, int m, FzScratch& f) {
+  int dev = 0, sms = 0;
+  GATO_CUDA_TRY(cudaGetDevice(&dev));
+  GATO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  f.sms = sms;
+  f.grid = (int)std::min<int64_t>(n / 64, 4 * (int64_t)sms);
+  f.nbf = (int)std::min<int64_t>((n / 4 + 255) / 256, 4 * sms);
+  const size_t vec = (size_t)n * sizeof(float);
+  const size_t dbl = (size_t)m * m + m + (m + 1) + (m + 2) + 2 + (size_t)2 * (m + 1) * f.grid + f.nbf;
+  unsigned char* p = (unsigned char*)stream_scratch(s, 3 * vec + dbl * sizeof(double) + 256, kSlotLanczosSweep);
+  if (!p) return fail(GATO_ENOMEM, "lanczos: sweep scratch allocation failed");
+  f.wh = (float*)p;
+  f.z = f.wh + n;
+  f.u = f.z + n;
+  double* d = (double*)(p + 3 * vec);
+  f.Cm = d;
+  f.dprev = f.Cm + (size_t)m * m;
+  f.c = f.dprev + m;
+  f.g = f.c + (m + 1);
+  f.binv = f.g + (m + 2);
+  f.part = f.binv + 2;
+  f.partn = f.part + (size_t)2 * (m + 1) * f.grid;
+  return GATO_OK;
+}
+
+std::atomic<int> g_lz_sweeps{1};   // 1: one basis sweep per step where supported, 2: two
+
+bool fz_ok(const float* Vb, int64_t n, int m, int passes) {
+  return g_lz_sweeps.load() == 1 && passes == 1 && m <= kFzMaxM && n % kFzCE == 0 && n / kFzCE >= 1 &&
+         ((uintptr_t)Vb % 16) == 0;
+}
+
+__global__ void k_fz_init(double* g, double* binv) {
+  g[0] = 0.0;
+  binv[0] = 1.0;
+  binv[1] = 1.0;
+}
+
+int lanczos_fused(gato_operator& op, const void* psi0, int m, int K, double tol, float* Vb, double* evals,
+                  float* evecs, double* alphas, double* betas, int* flag, cudaStream_t s) {
+  const int64_t n = op_n3(op);
+  const double dV = op.dV;
+  LzScratch z;
+  GATO_TRY(lz_scratch(s, n, m, K, z, false));
+  FzScratch f;
+  GATO_TRY(fz_scratch(s, n, m, f));
+  GATO_TRY(lz_begin<float>(psi0, Vb, n, dV, z, s));
+  GATO_TRY(op_apply(op, Vb, f.z, s));   // F v_0
+  k_fz_init<<<1, 1, 0, s>>>(f.g, f.binv);
+  GATO_LAUNCH_TRY();
+  {
+    static std::atomic<unsigned> done{0};   // the carve-out, once per device
+    int dev = 0;
+    GATO_CUDA_TRY(cudaGetDevice(&dev));
+    if (!(done.load() & (1u << (dev & 31)))) {
+      GATO_CUDA_TRY(cudaFuncSetAttribute(k_fz_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kFzSmemCap));
+      done.fetch_or(1u << (dev & 31));
+    }
+  }
+  if (n > INT32_MAX) return fail(GATO_EUNSUPPORTED, "lanczos: field too large for the sweep's tensor map");
+  for (int j = 0; j < m; ++j) {
+    const float* wh = j == 0 ? Vb : f.wh;   // v_0 itself (beta = 1, c = g = 0) at the first step
+    const int ce = fz_ce(j, n);
+    alignas(64) unsigned char tm[128];
+    TmaBox bx;
+    bx.rank = 2;
+    bx.dims[0] = (uint64_t)n;
+    bx.dims[1] = (uint64_t)m + 1;
+    bx.strides_bytes[0] = (uint64_t)n * sizeof(float);
+    bx.box[0] = (uint32_t)fz_rw(j, ce);
+    bx.box[1] = j > 0 ? (uint32_t)j : 1u;   // unused at j = 0
+    GATO_TRY(encode_tma(tm, GATO_F32, Vb, bx));
+    const int nst = fz_stages(j, ce);
+    const size_t smj = fz_smem(j, ce, nst);
+    static int per_sm_of[kFzMaxM] = {};   // resident sweep blocks per SM, by step
+    if (per_sm_of[j] == 0) {
+      GATO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_of[j], k_fz_sweep, kFzThreads, smj));
+      if (per_sm_of[j] < 1) return fail(GATO_EUNSUPPORTED, "lanczos: sweep block does not fit");
+    }
+    const int G = (int)std::min<int64_t>(std::min<int64_t>(n / ce, (int64_t)std::min(per_sm_of[j], 4) * f.sms),
+                                         f.grid);
+    k_fz_sweep<<<G, kFzThreads, smj, s>>>(*reinterpret_cast<const CUtensorMap*>(tm), Vb, n, j, ce, nst, wh, f.z,
+                                          f.u, f.c, f.g, f.binv, f.part, device_error_word());
+    GATO_LAUNCH_TRY();
+    k_fz_post1<<<1, 512, 0, s>>>(f.part, G, j, dV, alphas, betas, f.dprev, f.Cm, m);
+    GATO_LAUNCH_TRY();
+    k_fz_form<<<f.nbf, 256, 0, s>>>(f.u, j > 0 ? Vb + (int64_t)(j - 1) * n : nullptr, Vb + (int64_t)j * n, f.wh, n,
+                                    betas, alphas, j, f.partn);
+    GATO_LAUNCH_TRY();
+    k_fz_post2<<<1, 256, 0, s>>>(f.partn, f.nbf, dV, f.Cm, m, j, alphas, betas, f.binv, f.c, f.g);
+    GATO_LAUNCH_TRY();
+    if (j + 1 < m) GATO_TRY(op_apply(op, f.wh, f.z, s));
+  }
+  return lz_finish<float>(Vb, n, m, K, tol, alphas, betas, evals, evecs, flag, z, s);
+}
+
 template <typename T>
 int lanczos_typed(gato_operator& op, const void* psi0, int m, int K, double tol, int passes,
                   void* krylov, double* evals, void* evecs, double* alphas, double* betas,
                   int* flag, cudaStream_t s) {
   const int64_t n = op_n3(op);
   T* Vb = (T*)krylov;
+  if constexpr (sizeof(T) == 4) {
+    if (fz_ok(Vb, n, m, passes))
+      return lanczos_fused(op, psi0, m, K, tol, Vb, evals, (float*)evecs, alphas, betas, flag, s);
+  }
   LzScratch z;
   GATO_TRY(lz_scratch(s, n, m, K, z, sizeof(T) == 8));
   GATO_TRY(lz_begin<T>(psi0, Vb, n, op.dV, z, s));
@@ -1132,4 +1585,13 @@ extern "C" int gato_lanczos_finish(int dtype, int64_t n, const void* krylov, int
   if (dtype == GATO_F64)
     return lz_finish<double>((const double*)krylov, n, m, K, tol, alphas_dev, betas_dev, evals_dev, (double*)evecs, flag_dev, z, s);
   return lz_finish<float>((const float*)krylov, n, m, K, tol, alphas_dev, betas_dev, evals_dev, (float*)evecs, flag_dev, z, s);
+}
+
+// Tuning (no reference counterpart): sweeps of the basis per Lanczos step on the FP32 path,
+// 1 (the one-sweep form, where m <= 200 and n is a multiple of 128) or 2 (classical
+// Gram-Schmidt: coefficient sweep, then correction sweep).
+extern "C" int gato_lanczos_tune(int sweeps) {
+  if (sweeps != 1 && sweeps != 2) return fail(GATO_EBADARG, "gato_lanczos_tune: sweeps must be 1 or 2");
+  g_lz_sweeps.store(sweeps);
+  return GATO_OK;
 }

@@ -219,6 +219,12 @@ int gato_op_energy_terms(gato_op_t op, const void* V_ext, double* terms_dev, voi
 int gato_lanczos(gato_op_t op, const void* psi0, int m, int K, double tol, int reorth_passes,
                  void* krylov, double* evals_dev, void* evecs, double* alphas_dev,
                  double* betas_dev, int* flag_dev, void* stream);
+/* Tuning (no reference counterpart): basis sweeps per step of the FP32
+ * Lanczos loop: 1 = one sweep (the operator applied to the unorthogonalised
+ * three-term vector, its image recovered from the Lanczos relation; used
+ * where m <= 200 and n is a multiple of 128), 2 = the classical Gram-Schmidt
+ * coefficient and correction sweeps. Default 1.                          */
+int gato_lanczos_tune(int sweeps);
 /* The same algorithm in three pieces, for a matvec the caller supplies (the
  * duck-typed `H.apply` of lanczos.py:110-170): begin writes v_0 into slot 0;
  * the caller writes F v_j into slot j+1 and calls step(j), which
