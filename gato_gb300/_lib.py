@@ -75,6 +75,7 @@ _SIGS = {
     "gato_lanczos": [vp, vp, i32, i32, f64, i32, vp, vp, vp, vp, vp, vp, vp],
     "gato_lanczos_begin": [i32, i64, f64, vp, vp, i32, i32, vp],
     "gato_lanczos_step": [i32, i64, f64, vp, i32, i32, i32, i32, vp, vp, vp],
+    "gato_lanczos_tune": [i32],
     "gato_lanczos_finish": [i32, i64, vp, i32, i32, f64, vp, vp, vp, vp, vp, vp],
     "gato_hgh_local_grad": [i32, vp, i32, f64, i32, P_f64, P_f64, P_f64, P_f64, P_f64, vp],
     "gato_nonlocal_grad": [vp, vp, i32, P_f64, vp],

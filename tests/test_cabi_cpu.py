@@ -52,6 +52,8 @@ def test_validation_maps_to_reference_exceptions():
         _lib.check(L.gato_lanczos(None, None, 10, 4, 1e-10, 1, None, None, None, None, None, None, None))
     with pytest.raises(ValueError, match="rows per thread"):
         _lib.check(L.gato_stencil_tune(3))
+    with pytest.raises(ValueError, match="sweeps"):
+        _lib.check(L.gato_lanczos_tune(3))
     with pytest.raises(ValueError):
         _lib.boundary_code("mystery")
 

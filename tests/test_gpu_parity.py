@@ -473,6 +473,41 @@ def test_lanczos_vs_oracle_eigenvectors_and_generic_path():
     assert np.max(np.abs(S - np.eye(3))) < 1e-6
 
 
+@pytest.mark.parametrize("N", [24, 32])
+def test_lanczos_one_sweep_matches_two_sweep_and_oracle(N):
+    """The FP32 Lanczos in one basis sweep per step (the operator on the three-term vector, its image
+    from the Lanczos relation) against the two-sweep classical Gram-Schmidt form and the FP64 oracle:
+    Ritz values to FP32 accuracy, Ritz vectors orthonormal. m = 110 crosses every switch of chunk
+    width (j = 32, 99) and of threads per projection row (j = 32, 64)."""
+    from gato_gb300 import _lib
+    from gato_gb300.grid import Grid3D
+    from gato_gb300.hamiltonian import Hamiltonian
+    from gato_gb300.solvers.lanczos import lanczos
+    og, g = o.Grid3D(N, 10.0), Grid3D(N, 10.0)
+    X, Y, Z = og.coords()
+    # an anisotropic oscillator (omega 1, 1.3, 1.7): its lowest levels 2.0, 3.0, 3.3 Ha are simple,
+    # so FP32 rounding cannot seed a second copy of a degenerate level
+    V = 0.5 * (X ** 2 + 1.69 * Y ** 2 + 2.89 * Z ** 2)
+    psi0 = np.exp(-(X ** 2 + Y ** 2 + Z ** 2) / 2) * (1 + 0.1 * (X + Y + Z)) + 0.01 * np.sin(3 * X * Y)
+    m = 110
+    ref = o.lanczos(o.Hamiltonian(og, V, order=4), psi0, m, 3)
+    H = Hamiltonian(g, dev(V, torch.float32), order=4)
+    out = {}
+    try:
+        for sweeps in (1, 2):
+            _lib.call("gato_lanczos_tune", sweeps)
+            out[sweeps] = lanczos(H, dev(psi0, torch.float32), m, 3)
+    finally:
+        _lib.call("gato_lanczos_tune", 1)
+    for k in range(3):
+        e1, e2 = float(out[1].eigenvalues[k]), float(out[2].eigenvalues[k])
+        assert abs(e1 - e2) < 2e-5 * max(1.0, abs(e2)), (k, e1, e2)
+        assert abs(e1 - ref.eigenvalues[k]) < 2e-5 * max(1.0, abs(ref.eigenvalues[k])), (k, e1, ref.eigenvalues[k])
+    ev = host(out[1].eigenstates)
+    S = np.einsum("xyzi,xyzj->ij", ev, ev) * og.dV
+    assert np.max(np.abs(S - np.eye(3))) < 1e-4
+
+
 def test_lanczos_ho_ladder_kat():                        # reference test_lanczos.py:39-67
     from gato_gb300.grid import Grid3D
     from gato_gb300.hamiltonian import Hamiltonian
