@@ -45,6 +45,11 @@ int* device_error_word();
 // leaf operations while holding scratch uses its own slot.
 enum ScratchSlot { kSlotLeaf = 0, kSlotLanczos = 1, kSlotImagTime = 2, kSlotLanczosSweep = 3, kSlotCount = 4 };
 void* stream_scratch(cudaStream_t s, size_t bytes, int slot = kSlotLeaf);
+// Raise kernel fn's dynamic shared-memory limit to at least `bytes` on the current device. The
+// limit is one setting per kernel shared by every host thread, so it only ever grows (under a
+// lock): setting it to each launch's own size would let one thread lower it between another
+// thread's setting and launch, which then fails.
+int raise_smem_limit(const void* fn, size_t bytes);
 // Free every scratch slot of stream s (synchronises s first): for private
 // streams that are about to be destroyed.
 void release_stream_scratch(cudaStream_t s);

@@ -69,6 +69,20 @@ void* stream_scratch(cudaStream_t s, size_t bytes, int slot) {
   return p;
 }
 
+int raise_smem_limit(const void* fn, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> cur;
+  int dev = 0;
+  GATO_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  size_t& c = cur[{dev, fn}];
+  if (bytes > c) {
+    GATO_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    c = bytes;
+  }
+  return GATO_OK;
+}
+
 void free_after_pending(std::initializer_list<void*> ptrs) {
   bool any = false;
   for (void* p : ptrs) any = any || p != nullptr;

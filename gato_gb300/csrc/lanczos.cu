@@ -1017,7 +1017,7 @@ int lz_step(T* Vb, int64_t n, double dV, int j, int passes, double* alphas, doub
   const size_t smt = (size_t)(kLzThreads / 32) * nk * sizeof(double);
   const size_t smn = (size_t)nk * sizeof(double);
   if (smt > 48 * 1024)
-    GATO_CUDA_TRY(cudaFuncSetAttribute(k_gemv_t<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt));
+    GATO_TRY(raise_smem_limit(reinterpret_cast<const void*>(k_gemv_t<T, T>), smt));
   // alpha_j = dV <v_j, w'>
   k_gemv_t<T, T><<<z.nblk_t, kLzThreads, (kLzThreads / 32) * sizeof(double), s>>>(vj, n, 1, W, p1, n,
                                                                                   z.part);
@@ -1047,7 +1047,7 @@ int lz_finish(const T* Vb, int64_t n, int m, int K, double tol, const double* al
               cudaStream_t s) {
   const size_t sme = (size_t)3 * m * sizeof(double);
   if (sme > 48 * 1024)
-    GATO_CUDA_TRY(cudaFuncSetAttribute(k_tridiag_eig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sme));
+    GATO_TRY(raise_smem_limit(reinterpret_cast<const void*>(k_tridiag_eig), sme));
   k_tridiag_eig<<<K, 32, sme, s>>>(alphas, betas, m, K, evals, z.work, device_error_word());
   GATO_LAUNCH_TRY();
   k_tridiag_finish<<<1, 32, 0, s>>>(alphas, betas, m, K, evals, z.work, evals, z.Y, flag, tol);
@@ -1055,7 +1055,7 @@ int lz_finish(const T* Vb, int64_t n, int m, int K, double tol, const double* al
   constexpr int KB = 4;
   const size_t smr = (size_t)KB * m * sizeof(T);
   if (smr > 48 * 1024)
-    GATO_CUDA_TRY(cudaFuncSetAttribute(k_ritz<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smr));
+    GATO_TRY(raise_smem_limit(reinterpret_cast<const void*>(k_ritz<T, KB>), smr));
   for (int k0 = 0; k0 < K; k0 += KB) {
     k_ritz<T, KB><<<grid_for(n, 256, 152 * 8), 256, smr, s>>>(Vb, n, m, z.Y, k0, K, evecs, n);
     GATO_LAUNCH_TRY();
@@ -1463,16 +1463,7 @@ int lanczos_fused(gato_operator& op, const void* psi0, int m, int K, double tol,
   GATO_TRY(op_apply(op, Vb, f.z, s));   // F v_0
   k_fz_init<<<1, 1, 0, s>>>(f.g, f.binv);
   GATO_LAUNCH_TRY();
-  {
-    static std::atomic<unsigned> done{0};   // the carve-out, once per device
-    int dev = 0;
-    GATO_CUDA_TRY(cudaGetDevice(&dev));
-    if (!(done.load() & (1u << (dev & 31)))) {
-      GATO_CUDA_TRY(cudaFuncSetAttribute(k_fz_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kFzSmemCap));
-      done.fetch_or(1u << (dev & 31));
-    }
-  }
+  GATO_TRY(raise_smem_limit(reinterpret_cast<const void*>(k_fz_sweep), kFzSmemCap));
   if (n > INT32_MAX) return fail(GATO_EUNSUPPORTED, "lanczos: field too large for the sweep's tensor map");
   for (int j = 0; j < m; ++j) {
     const float* wh = j == 0 ? Vb : f.wh;   // v_0 itself (beta = 1, c = g = 0) at the first step
@@ -1488,12 +1479,14 @@ int lanczos_fused(gato_operator& op, const void* psi0, int m, int K, double tol,
     GATO_TRY(encode_tma(tm, GATO_F32, Vb, bx));
     const int nst = fz_stages(j, ce);
     const size_t smj = fz_smem(j, ce, nst);
-    static int per_sm_of[kFzMaxM] = {};   // resident sweep blocks per SM, by step
-    if (per_sm_of[j] == 0) {
-      GATO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_of[j], k_fz_sweep, kFzThreads, smj));
-      if (per_sm_of[j] < 1) return fail(GATO_EUNSUPPORTED, "lanczos: sweep block does not fit");
+    static std::atomic<int> per_sm_of[kFzMaxM];   // resident sweep blocks per SM, by step (0: unknown)
+    int per_sm = per_sm_of[j].load();
+    if (per_sm == 0) {
+      GATO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fz_sweep, kFzThreads, smj));
+      if (per_sm < 1) return fail(GATO_EUNSUPPORTED, "lanczos: sweep block does not fit");
+      per_sm_of[j].store(per_sm);
     }
-    const int G = (int)std::min<int64_t>(std::min<int64_t>(n / ce, (int64_t)std::min(per_sm_of[j], 4) * f.sms),
+    const int G = (int)std::min<int64_t>(std::min<int64_t>(n / ce, (int64_t)std::min(per_sm, 4) * f.sms),
                                          f.grid);
     k_fz_sweep<<<G, kFzThreads, smj, s>>>(*reinterpret_cast<const CUtensorMap*>(tm), Vb, n, j, ce, nst, wh, f.z,
                                           f.u, f.c, f.g, f.binv, f.part, device_error_word());

@@ -273,8 +273,7 @@ __global__ void __launch_bounds__(kFftThreads)
 
 template <typename KernelT>
 int set_smem(KernelT k, size_t bytes) {
-  GATO_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-  return GATO_OK;
+  return raise_smem_limit(reinterpret_cast<const void*>(k), bytes);
 }
 
 template <typename T2>
@@ -300,7 +299,7 @@ int launch_cols(int mode, const T2* in, T2* out, const ColGeom& g, int outer, in
 
 template <typename T>
 int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, double* energy_dev,
-              cudaStream_t s) {
+              cudaStream_t s, cudaEvent_t join) {
   using T2 = typename Cplx<T>::type;
   const int N = pl.N, M = pl.M;
   const int64_t nrows = (int64_t)N * N;
@@ -381,6 +380,7 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
       GATO_TRY(fast::cols<T>(M, COL_FMI, S2, S2, gx, M, nfg, tw2, (const T*)pl.ghat, pl.H, s));
       GATO_TRY(fast::cols<T>(M, COL_INV, S2, S1, gyi, N, nfg, tw2, nullptr, pl.H, s));
       }
+      if (join && g == 0 && epi == EPI_ACC) GATO_CUDA_TRY(cudaStreamWaitEvent(s, join, 0));
       if (epi == EPI_J)
         GATO_TRY(fast::rows_inv_j<T>(M, args, f0, nfg, S1, tw2, s));
       else
@@ -400,6 +400,7 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
     // 4. y inverse: S2[f][x][ky][kz] -> S1[f][x][y<N][kz]
     GATO_TRY(launch_cols<T2>(COL_INV, S2, S1, gyi, N, nfg, pl.fp, tw, nullptr, pl.H, s));
     // 5. z inverse + epilogue
+    if (join && g == 0 && epi == EPI_ACC) GATO_CUDA_TRY(cudaStreamWaitEvent(s, join, 0));
     if (epi == EPI_ENERGY)
       k_rows_inv<T, true><<<nblk_i, kFftThreads, sm_i, s>>>(args, f0, nfg, S1, pl.fp, tw, N, Li, 0,
                                                             part, sstride);
@@ -419,11 +420,14 @@ int run_typed(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate, d
 }  // namespace
 
 int poisson_run(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate,
-                double* energy_dev, cudaStream_t s) {
-  if (args.nf <= 0) return GATO_OK;
+                double* energy_dev, cudaStream_t s, cudaEvent_t join) {
+  if (args.nf <= 0) {
+    if (join) GATO_CUDA_TRY(cudaStreamWaitEvent(s, join, 0));
+    return GATO_OK;
+  }
   if (args.nf > kMaxFields) return fail(GATO_EBADARG, "poisson: too many fields (%d)", args.nf);
-  if (pl.dtype == GATO_F64) return run_typed<double>(pl, args, epi, accumulate, energy_dev, s);
-  return run_typed<float>(pl, args, epi, accumulate, energy_dev, s);
+  if (pl.dtype == GATO_F64) return run_typed<double>(pl, args, epi, accumulate, energy_dev, s, join);
+  return run_typed<float>(pl, args, epi, accumulate, energy_dev, s, join);
 }
 
 static int plan_create(int dtype, int N, double h, double eps, int max_fields, PoissonPlan& pl,

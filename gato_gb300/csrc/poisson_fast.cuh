@@ -1,6 +1,7 @@
 // Pair-solve pipeline kernels on the register-resident two-pass FFT engine
 // (fft2.cuh), one instantiation per supported doubled-grid size M.
 #pragma once
+#include <atomic>
 #include "fft2.cuh"
 #include "poisson.cuh"
 #include "ptx.cuh"
@@ -676,8 +677,7 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
 
 template <typename K>
 inline int smem_attr(K k, size_t bytes) {
-  GATO_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-  return GATO_OK;
+  return raise_smem_limit(reinterpret_cast<const void*>(k), bytes);
 }
 
 // Launchers for one shape.
@@ -764,16 +764,18 @@ struct Launch {
         auto kern = k_rows_fwd_pers<T, R1, R2, LM>;
         const size_t smp = sm + stage_bytes;   // a second staging slot
         GATO_TRY(smem_attr(kern, smp));
-        static int per_sm[kMaxIn + 1] = {}, sms = 0;   // resident CTAs per SM by staged inputs
-        int& ps = per_sm[ri.nin];
-        if (ps == 0) {
-          int dev = 0;
+        static std::atomic<int> wave[kMaxIn + 1];   // resident blocks of one wave by staged inputs (0: unknown)
+        int w = wave[ri.nin].load();
+        if (w == 0) {
+          int dev = 0, sms = 0, ps = 0;
           GATO_CUDA_TRY(cudaGetDevice(&dev));
           GATO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
           GATO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ps, kern, LM * Shape<R1, R2>::RMAX, smp));
           if (ps < 1) return fail(GATO_EUNSUPPORTED, "z forward: no resident CTA fits");
+          w = ps * sms;
+          wave[ri.nin].store(w);
         }
-        const unsigned pg = (unsigned)std::min<int64_t>(grid, (int64_t)ps * sms);
+        const unsigned pg = (unsigned)std::min<int64_t>(grid, (int64_t)w);
         kern<<<pg, LM * Shape<R1, R2>::RMAX, smp, s>>>(a, ri, f0, nfg, S1, tw, device_error_word());
       } else if (bulk) {
         GATO_TRY(smem_attr(k_rows_fwd_multi<T, R1, R2, LM, true>, sm));

@@ -15,6 +15,8 @@
 // directly; the y forward reads and the y inverse writes the complex rows
 // (AoS) of S1 that the z passes use.
 #pragma once
+#include <atomic>
+
 #include <cuda.h>
 
 #include "fft2p.cuh"
@@ -192,17 +194,21 @@ struct LaunchP {
     using G = PGeom<R1, R2, LPR, MODE>;
     auto kern = k_colsp<R1, R2, LPR, MODE>;
     // one resident wave of persistent CTAs (blocks per SM from the occupancy calculator)
-    static int per_sm = 0, sms = 0;
+    // the resident blocks of one wave (blocks per SM x SMs), computed once; read by any thread
+    static std::atomic<int> wave{0};
     GATO_TRY(fast::smem_attr(kern, G::SMEM));
-    if (per_sm == 0) {
-      int dev = 0;
+    int w = wave.load();
+    if (w == 0) {
+      int dev = 0, sms = 0, per_sm = 0;
       GATO_CUDA_TRY(cudaGetDevice(&dev));
       GATO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
       GATO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, G::NT, G::SMEM));
       if (per_sm < 1) return fail(GATO_EUNSUPPORTED, "packed column pass: no resident CTA fits");
+      w = per_sm * sms;
+      wave.store(w);
     }
     const int64_t ntiles = (int64_t)nf * outer * (g.ncols / CW);
-    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, (int64_t)per_sm * sms);
+    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, (int64_t)w);
     kern<<<grid, G::NT, G::SMEM, s>>>(tin, tg, out, g, outer, nf, tw4, device_error_word());
     GATO_LAUNCH_TRY();
     return GATO_OK;
