@@ -55,6 +55,7 @@ _SIGS = {
     "gato_poisson_stage": [vp, i32, i32, vp],
     "gato_poisson_tune": [vp, i32, i32],
     "gato_op_tune": [vp, i32],
+    "gato_op_overlap": [vp, i32],
     "gato_density": [i32, vp, i32, i64, vp, vp],
     "gato_mix": [i32, vp, vp, i64, f64, vp],
     "gato_exchange_apply": [vp, vp, vp, i32, vp, f64, vp],

@@ -3,6 +3,9 @@
 //
 // apply      : stencil(+V) writes out; V_nl scatter-adds; the exchange pass
 //              subtracts sum_j phi_j J[phi_j psi] in its final z-row epilogue.
+//              The stencil and V_nl run on the operator's side stream beside
+//              the exchange's transforms and join before the epilogue (in the
+//              block apply: before the pair pass).
 // apply_block: F phi_i for every occupied orbital with the n(n+1)/2 pair
 //              potentials J[phi_i phi_j], each feeding both phi_i and phi_j:
 //              either the pipeline writes the J_ij fields and one elementwise
@@ -51,17 +54,46 @@ __global__ void k_sum_scaled(const double* in, int n, double scale, double* out)
 
 }  // namespace
 
-int op_apply(gato_operator& op, const void* in, void* out, cudaStream_t s) {
-  const double coef = -0.5 / (op.h * op.h);
-  GATO_TRY(stencil_apply(op.dtype, in, op.V, out, 1, op.N, op.N, op.N, op_n3(op), coef, op.boundary,
-                         op.order, nullptr, op.dV, s));
-  if (op.nl) GATO_TRY(nonlocal_apply(op.nl->n, in, out, 1, s));
-  if (op.n_orb > 0) {
-    PassArgs a;
-    GATO_TRY(exchange_args(a, in, op.orbitals, op.n_orb, op_esize(op), op_n3(op), out, -1.0));
-    GATO_TRY(poisson_run(op.pp->p, a, EPI_ACC, true, nullptr, s));
-  }
+// The operator's side stream and its fork/join events, created on first use.
+static int op_side(gato_operator& op) {
+  if (op.side) return GATO_OK;
+  GATO_CUDA_TRY(cudaStreamCreateWithFlags(&op.side, cudaStreamNonBlocking));
+  GATO_CUDA_TRY(cudaEventCreateWithFlags(&op.ev_fork, cudaEventDisableTiming));
+  GATO_CUDA_TRY(cudaEventCreateWithFlags(&op.ev_join, cudaEventDisableTiming));
   return GATO_OK;
+}
+
+// out[b] = (-1/2 L + V) psi[b] (+ V_nl psi[b]) for nb fields, on stream ls.
+static int local_part(gato_operator& op, const void* in, void* out, int nb, cudaStream_t ls) {
+  const double coef = -0.5 / (op.h * op.h);
+  GATO_TRY(stencil_apply(op.dtype, in, op.V, out, nb, op.N, op.N, op.N, op_n3(op), coef, op.boundary,
+                         op.order, nullptr, op.dV, ls));
+  if (op.nl) GATO_TRY(nonlocal_apply(op.nl->n, in, out, nb, ls));
+  return GATO_OK;
+}
+
+// Runs the local part on the side stream from this point of s; returns the join event
+// (null when the local part ran on s itself).
+static int fork_local(gato_operator& op, const void* in, void* out, int nb, cudaStream_t s,
+                      cudaEvent_t* join) {
+  *join = nullptr;
+  if (!op.overlap) return local_part(op, in, out, nb, s);
+  GATO_TRY(op_side(op));
+  GATO_CUDA_TRY(cudaEventRecord(op.ev_fork, s));
+  GATO_CUDA_TRY(cudaStreamWaitEvent(op.side, op.ev_fork, 0));
+  GATO_TRY(local_part(op, in, out, nb, op.side));
+  GATO_CUDA_TRY(cudaEventRecord(op.ev_join, op.side));
+  *join = op.ev_join;
+  return GATO_OK;
+}
+
+int op_apply(gato_operator& op, const void* in, void* out, cudaStream_t s) {
+  if (op.n_orb <= 0) return local_part(op, in, out, 1, s);
+  cudaEvent_t join = nullptr;
+  GATO_TRY(fork_local(op, in, out, 1, s, &join));
+  PassArgs a;
+  GATO_TRY(exchange_args(a, in, op.orbitals, op.n_orb, op_esize(op), op_n3(op), out, -1.0));
+  return poisson_run(op.pp->p, a, EPI_ACC, true, nullptr, s, join);
 }
 
 static void block_pairs(PassArgs& a, const gato_operator& op, void* out, bool energy) {
@@ -162,7 +194,13 @@ extern "C" int gato_op_create(int dtype, int N, double h, int order, int boundar
 
 extern "C" int gato_op_destroy(gato_op_t op) {
   if (!op) return GATO_OK;
-  free_after_pending({op->dscratch, op->rho, op->jbuf});
+  free_after_pending({op->dscratch, op->rho, op->jbuf});   // waits for the device first
+  if (op->side) {
+    cudaStreamSynchronize(op->side);
+    cudaStreamDestroy(op->side);
+    cudaEventDestroy(op->ev_fork);
+    cudaEventDestroy(op->ev_join);
+  }
   delete op;
   return GATO_OK;
 }
@@ -203,10 +241,8 @@ extern "C" int gato_op_apply_block(gato_op_t op, void* out, void* stream) {
   if (!op || !out || op->n_orb < 1) return fail(GATO_EBADARG, "gato_op_apply_block: needs orbitals");
   if (op->n_orb > kMaxOut) return fail(GATO_EUNSUPPORTED, "block apply: at most %d orbitals", kMaxOut);
   cudaStream_t s = as_stream(stream);
-  const double coef = -0.5 / (op->h * op->h);
-  GATO_TRY(stencil_apply(op->dtype, op->orbitals, op->V, out, op->n_orb, op->N, op->N, op->N,
-                         op_n3(*op), coef, op->boundary, op->order, nullptr, op->dV, s));
-  if (op->nl) GATO_TRY(nonlocal_apply(op->nl->n, op->orbitals, out, op->n_orb, s));
+  cudaEvent_t join = nullptr;
+  GATO_TRY(fork_local(*op, op->orbitals, out, op->n_orb, s, &join));
   PassArgs a;
   block_pairs(a, *op, out, false);
   if (op->block_epi != 2 && poisson_j_supported(op->pp->p)) {
@@ -222,9 +258,16 @@ extern "C" int gato_op_apply_block(gato_op_t op, void* out, void* stream) {
     a.jbase = op->jbuf;
     a.jstride = op_n3(*op);
     GATO_TRY(poisson_run(op->pp->p, a, EPI_J, false, nullptr, s));
+    if (join) GATO_CUDA_TRY(cudaStreamWaitEvent(s, join, 0));
     return pair_exchange(op->dtype, op->orbitals, op->n_orb, op->jbuf, out, op_n3(*op), s);
   }
-  return poisson_run(op->pp->p, a, EPI_ACC, true, nullptr, s);
+  return poisson_run(op->pp->p, a, EPI_ACC, true, nullptr, s, join);
+}
+
+extern "C" int gato_op_overlap(gato_op_t op, int on) {
+  if (!op || (on != 0 && on != 1)) return fail(GATO_EBADARG, "gato_op_overlap: on must be 0 or 1");
+  op->overlap = on;
+  return GATO_OK;
 }
 
 extern "C" int gato_op_tune(gato_op_t op, int block_epilogue) {

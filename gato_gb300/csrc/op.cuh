@@ -19,6 +19,11 @@ struct gato_operator {
   void* jbuf = nullptr;         // pair potentials J_ij of the block apply
   size_t jbuf_bytes = 0;
   int block_epi = 0;            // block apply epilogue: 0 auto, 1 J fields + pair pass, 2 fused
+  // The local part (stencil + V, non-local projectors) runs on a side stream beside the exchange's
+  // transforms and joins before the first kernel that touches the outputs again.
+  int overlap = 1;
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 namespace gato {

@@ -76,6 +76,11 @@ class Operator:
         _lib.call("gato_op_tune", self.handle, int(block_epilogue))
         self.block_epilogue = int(block_epilogue)
 
+    def overlap(self, on: bool):
+        """Run the stencil and non-local part beside the exchange transforms (True, the default) or
+        in order on the caller's stream (False); results are the same either way."""
+        _lib.call("gato_op_overlap", self.handle, int(bool(on)))
+
     def set_potential(self, V: torch.Tensor | None):
         self._keep["V"] = V
         _lib.call("gato_op_set_potential", self.handle, C.c_void_p(V.data_ptr() if V is not None else None))

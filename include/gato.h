@@ -189,6 +189,13 @@ int gato_op_destroy(gato_op_t op);
 int gato_op_set_potential(gato_op_t op, const void* V);
 int gato_op_set_nonlocal(gato_op_t op, gato_nonlocal_t nl);
 int gato_op_set_exchange(gato_op_t op, gato_poisson_t plan, const void* orbitals, int n_orb);
+/* Tuning (no reference counterpart): 1 (default) runs the stencil and the
+ * non-local projectors of an apply on the operator's own side stream,
+ * concurrently with the exchange's FFT passes, joined before the first
+ * kernel that accumulates into the outputs; 0 runs everything on the
+ * caller's stream in order. Either way the call is ordered on the caller's
+ * stream like any other launch.                                          */
+int gato_op_overlap(gato_op_t op, int on);
 /* Block-apply epilogue: 0 = auto, 1 = J_ij fields then one pair pass, 2 =
  * accumulate every output in the z-inverse epilogue. No reference
  * counterpart (a tuning knob of this library, set by the autotuner).      */

@@ -316,6 +316,30 @@ def test_block_fock_epilogues(dtype, epilogue):
 
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_local_part_overlap_is_bitwise_neutral(dtype):
+    """The stencil and non-local part on the operator's side stream (beside the exchange transforms)
+    give bit-identical block applies, matvecs and graph replays to the in-order launches."""
+    _, F, fields = _water_fock(dtype)
+    op = F._gato_operator(dtype, allow_generic=True)
+    res = {}
+    for on in (0, 1):
+        op.overlap(on)
+        blk = op.apply_block().clone()
+        mv = op.apply(fields[1].contiguous()).clone()
+        out = torch.empty_like(fields)
+        g = op.block_graph(out)
+        out.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        res[on] = (blk, mv, out.clone())
+    op.overlap(1)
+    for a, b in zip(res[0], res[1]):
+        assert torch.equal(a, b)
+    assert rel_err(host(res[1][0]), GOLD["water_block_fock"]) < (1e-11 if dtype == torch.float64 else 3e-5)
+    assert torch.equal(res[1][0], res[1][2])
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_block_fock_per_field_z_forward(dtype):
     """Engine 2 (one z-forward CTA per field) gives the golden block apply too."""
     from gato_gb300.autotune import set_plan
