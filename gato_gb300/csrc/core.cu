@@ -43,7 +43,10 @@ int* device_error_word() {
   if (it != g_err_words.end()) return it->second;
   int* p = nullptr;
   if (cudaMalloc(&p, sizeof(int)) != cudaSuccess) return nullptr;
-  if (cudaMemset(p, 0, sizeof(int)) != cudaSuccess) return nullptr;
+  // cleared on the legacy stream and waited for: kernels on non-blocking streams write it next
+  if (cudaMemsetAsync(p, 0, sizeof(int), cudaStreamLegacy) != cudaSuccess ||
+      cudaStreamSynchronize(cudaStreamLegacy) != cudaSuccess)
+    return nullptr;
   g_err_words[dev] = p;
   return p;
 }

@@ -334,6 +334,7 @@ __global__ void __launch_bounds__(kBulkThreads)
 #pragma unroll
         for (int u = 0; u < G::VEC; ++u) v[g * G::VEC + u] = qe[u];
       }
+      fence_proxy_async_smem();   // the slot's reads are done before the next bulk copy lands
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[t % kBulkStages]);
       T sk = (T)0;
@@ -464,6 +465,7 @@ __global__ void __launch_bounds__(kBulkThreads, 3)
 #pragma unroll
           for (int u = 0; u < G::VEC; ++u) v[g * G::VEC + u] = qe[u];
         }
+        fence_proxy_async_smem();   // the slot's reads are done before the next bulk copy lands
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[t % kBulkStages]);
         ++t;
@@ -551,6 +553,7 @@ __global__ void __launch_bounds__(kBulkThreads)
 #pragma unroll
         for (int u = 0; u < G::VEC; ++u) v[g * G::VEC + u] = qe[u];
       }
+      fence_proxy_async_smem();   // the slot's reads are done before the next bulk copy lands
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[t % kBulkStages]);
       const float ck = cs[k];
@@ -1297,6 +1300,7 @@ __global__ void __maxnreg__(96)
       accA += (double)sa;
       accD += (double)sd;
     }
+    fence_proxy_async_smem();   // the chunk's reads and writes of bf precede the next copy into it
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[b]);
   }

@@ -456,8 +456,11 @@ static int plan_create(int dtype, int N, double h, double eps, int max_fields, P
     tw32[k] = make_float2((float)tw64[k].x, (float)tw64[k].y);
   }
   GATO_CUDA_TRY(cudaMalloc(&pl.tw, (size_t)M * 2 * ts));
-  GATO_CUDA_TRY(cudaMemcpy(pl.tw, dtype == GATO_F64 ? (void*)tw64.data() : (void*)tw32.data(),
-                           (size_t)M * 2 * ts, cudaMemcpyHostToDevice));
+  // uploads go on s: a blocking cudaMemcpy from pageable memory may return before its DMA lands
+  // and is not ordered against a non-blocking s, whose kernels read these tables next (a pageable
+  // cudaMemcpyAsync returns once the host data is staged, so the vectors may go out of scope)
+  GATO_CUDA_TRY(cudaMemcpyAsync(pl.tw, dtype == GATO_F64 ? (void*)tw64.data() : (void*)tw32.data(),
+                                (size_t)M * 2 * ts, cudaMemcpyHostToDevice, s));
   if (const int R2 = fast::shape_r2(M)) {
     // the register engine's stage twiddles: row k1 holds exp(-2 pi i n2 k1 / M)
     // for n2 < R2, rows padded to the stride the kernels read them with
@@ -473,8 +476,8 @@ static int plan_create(int dtype, int N, double h, double eps, int max_fields, P
       }
     const size_t bytes = (size_t)R1 * S * 2 * ts;
     GATO_CUDA_TRY(cudaMalloc(&pl.tw2, bytes));
-    GATO_CUDA_TRY(cudaMemcpy(pl.tw2, dtype == GATO_F64 ? (void*)t64.data() : (void*)t32.data(), bytes,
-                             cudaMemcpyHostToDevice));
+    GATO_CUDA_TRY(cudaMemcpyAsync(pl.tw2, dtype == GATO_F64 ? (void*)t64.data() : (void*)t32.data(), bytes,
+                                  cudaMemcpyHostToDevice, s));
   }
   if (const int R2 = dtype == GATO_F32 ? fast::packed_r2(M) : 0) {
     // packed stage twiddles: entry k1 R2 + n2 = (c, c, s, s), (c, s) = exp(-2 pi i n2 k1 / M)
@@ -486,11 +489,11 @@ static int plan_create(int dtype, int N, double h, double eps, int max_fields, P
         t4[(size_t)k1 * R2 + n2] = make_float4(c, c, sn, sn);
       }
     GATO_CUDA_TRY(cudaMalloc(&pl.tw4, t4.size() * sizeof(float4)));
-    GATO_CUDA_TRY(cudaMemcpy(pl.tw4, t4.data(), t4.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    GATO_CUDA_TRY(cudaMemcpyAsync(pl.tw4, t4.data(), t4.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
   }
   double2* tw_d = nullptr;
   GATO_CUDA_TRY(cudaMalloc(&tw_d, (size_t)M * sizeof(double2)));
-  GATO_CUDA_TRY(cudaMemcpy(tw_d, tw64.data(), (size_t)M * sizeof(double2), cudaMemcpyHostToDevice));
+  GATO_CUDA_TRY(cudaMemcpyAsync(tw_d, tw64.data(), (size_t)M * sizeof(double2), cudaMemcpyHostToDevice, s));
   // kernel spectrum in FP64 on an M^3 complex scratch
   double2* X = nullptr;
   const size_t xbytes = (size_t)M * M * M * sizeof(double2);

@@ -138,8 +138,11 @@ bool poisson_fe_supported(const PoissonPlan& pl);
 // at most plan.max_fields. EPI_ACC: out[o] = (accumulate ? out[o] : 0) +
 // sum of terms. EPI_ENERGY: energy_dev[slot] = dV * sum of weighted terms
 // (two slots).
+// join (EPI_ACC only, may be null): the stream waits on it before the first z-inverse epilogue,
+// the first kernel that reads or writes the outputs (work on another stream that also writes them,
+// ordered before the accumulation without holding up the transforms).
 int poisson_run(PoissonPlan& pl, const PassArgs& args, int epi, bool accumulate,
-                double* energy_dev, cudaStream_t s);
+                double* energy_dev, cudaStream_t s, cudaEvent_t join = nullptr);
 
 }  // namespace gato
 

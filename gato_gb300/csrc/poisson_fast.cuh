@@ -493,6 +493,7 @@ __global__ void __launch_bounds__(L * Shape<R1, R2>::RMAX)
         }
         row_fwd_stage1<T2, R1, R2, true>(buf, line, j, v);
       }
+      fence_proxy_async_smem();   // this slot's reads precede the copies issued into it next
       __syncthreads();
       if (j < R1) {
         T2 X[R2];

@@ -133,7 +133,10 @@ __global__ void __launch_bounds__(PGeom<R1, R2, LPR, MODE>::NT)
 #pragma unroll
       for (int k2 = 0; k2 < R2; ++k2) X[k2] = fft2p::from_split(stage[(q + R1 * k2) * LPR + pr]);
     }
-    __syncthreads();   // the staged input is consumed: the next tile's copies may land on it
+    // the staged input (and the previous tile's kernel block) is consumed: the next tile's copies
+    // may land on it once every thread's generic reads are ordered before the async proxy
+    fence_proxy_async_smem();
+    __syncthreads();
     if (t == 0 && tile + (int)gridDim.x < ntiles) issue(tile + gridDim.x, slot ^ 1);
     if (MODE != COL_INV && q < R1) {
 #pragma unroll

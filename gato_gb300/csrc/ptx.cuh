@@ -25,6 +25,14 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                : "memory");
 }
 
+// Orders this thread's earlier generic-proxy accesses of shared memory before later async-proxy
+// (TMA / bulk copy) accesses. A barrier or mbarrier arrival alone orders generic accesses between
+// threads only: every thread that read or wrote a copy destination executes this before the
+// barrier (or arrival) after which the next copy into that buffer is issued.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 // Plain arrival (release semantics at CTA scope: this thread's earlier
 // shared-memory reads are ordered before it).
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {

@@ -276,6 +276,7 @@ __global__ void __launch_bounds__(kZP*(kBY / YPT))
       if constexpr (STORE) op += pstride;
     }
     // every thread is done with plane q - R; a timed-out wait anywhere stops the CTA
+    fence_proxy_async_smem();   // its slot's reads precede the copy issued into it below
     if (__syncthreads_or(bad)) {
       bad = true;
       return false;

@@ -45,3 +45,72 @@ def test_batch_worker_error_surfaces():
     bad = SystemSpec("H3", Nuclei(pos, torch.ones(3, dtype=torch.float64)), 32, 0.25, (lookup("H"),) * 3)
     with pytest.raises(ValueError):
         solve_batch([good, bad], streams=2, max_iters=5)
+
+
+def test_threads_on_packed_shapes_are_bitwise_stable():
+    """Four threads, each on its own stream, drive FP32 operators on 64^3 and 96^3 grids (the
+    packed column passes, the persistent z forward, the stencil's TMA ring and the cluster
+    non-local apply all run concurrently on shared SMs). Every apply, block apply and energy-term
+    evaluation must equal the single-threaded result bit for bit: a shared-memory buffer that a
+    copy engine refills while another kernel's loads still queue behind it would show up here."""
+    import threading
+    from gato_gb300 import scf
+    from gato_gb300.batch import draw_systems
+    from gato_gb300.solvers.poisson import get_plan
+    f32 = torch.float32
+    specs = draw_systems(10, seed=0, grids=(64, 96))
+    picked = [next(s for s in specs if s.N == 96 and s.n_occ() == 4),
+              next(s for s in specs if s.N == 64 and s.n_occ() == 4)]
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    cases = []
+    for sp in picked:
+        shape = sp.grid.shape
+        cases.append((sp, torch.randn(shape, device="cuda", dtype=f32, generator=gen),
+                      torch.randn(shape, device="cuda", dtype=f32, generator=gen),
+                      0.01 * torch.randn((4,) + shape, device="cuda", dtype=f32, generator=gen),
+                      torch.randn(shape, device="cuda", dtype=f32, generator=gen)))
+
+    def run(case, overlap):
+        sp, V, Vx, orb, psi = case
+        model, grid = sp.model(), sp.grid
+        nl = scf._native_nl(model.nonlocal_op(sp.nuclei, grid, f32), grid, f32)
+        op = scf.Operator(grid, f32)
+        op.overlap(overlap)
+        op.set_nonlocal(nl)
+        op.set_potential(V)
+        op.set_exchange(get_plan(grid.N, grid.h, model.epsilon(grid), f32, scf.pair_fields(4)), orb)
+        return [op.apply(psi), op.apply_block(), op.energy_terms(Vx)], op
+
+    refs = []
+    for c in cases:
+        outs, _ = run(c, True)
+        torch.cuda.synchronize()
+        refs.append([t.clone() for t in outs])
+    mismatches, errors = [], []
+
+    def worker(k):
+        try:
+            s = torch.cuda.Stream()
+            keep, outs = [], []
+            with torch.cuda.stream(s):
+                for i in range(12):
+                    ci = (i + k) % len(cases)
+                    r, op = run(cases[ci], overlap=(i // 2) % 2 == 0)
+                    keep.append(op)
+                    outs.append((ci, r))
+                s.synchronize()
+            for ci, r in outs:
+                for j, name in enumerate(("apply", "block", "energy")):
+                    if not torch.equal(r[j], refs[ci][j]):
+                        mismatches.append((k, picked[ci].name, name))
+        except BaseException as e:   # reported after the join
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(k,)) for k in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    torch.cuda.synchronize()
+    assert not errors, errors
+    assert not mismatches, mismatches[:8]
