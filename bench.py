@@ -32,9 +32,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_DEFAULT, H_DEFAULT, N_OCC = 128, 0.25, 4
-# DRAM read + write of one x-pass launch (5 fields, 128^3) in the ncu capture
-# summarised in profiles/block_fock_apply_h2o128_f32_kernels.md
-FMI_TRAFFIC_128 = 345_241_088 + 275_777_792
+# DRAM read + write of one x-pass launch (5 fields, 128^3) in the one-kernel ncu capture summarised
+# in profiles/x_pass_fmi_h2o128_f32_packed.md (a recorded figure, not measured by this run)
+FMI_TRAFFIC_128 = 366_578_176 + 274_962_176
+FMI_TRAFFIC_SOURCE = "profiles/x_pass_fmi_h2o128_f32_packed.md (ncu, same kernel and workload; not re-measured here)"
+FMI_LIMITER = ("packed two-line FFT, 3 CTAs/SM by shared memory (~10 warps): FMA pipe 58%, shared-memory "
+               "wavefronts ~60%, issue 44% (ncu); HBM 0.57")
 METRIC = "H2O 128^3 RHF block Fock-applies/s (mixed FP32/FP64 at |dE|<1uHa) and force time"
 UNIT = "Fock-applies/s"
 
@@ -117,7 +120,7 @@ def energy_gate_160():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled every 200 ms during a region."""
+    """nvidia-smi clocks/throttle reasons sampled every 50 ms during a region."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -130,9 +133,15 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "50"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+        # the region starts once sampling has (nvidia-smi takes a moment to start)
+        t0 = time.time()
+        while self.proc is not None and time.time() - t0 < 3.0:
+            if os.path.exists(self.path) and os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.01)
         return self
 
     def __exit__(self, *exc):
@@ -441,7 +450,18 @@ def run_gato(args):
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    # the step as direct launches, then as a replay of the same launches captured once in a CUDA graph
+    # the step as direct launches, then as a replay of the same launches captured once in a CUDA graph;
+    # clocks are sampled over both, bracketed by 0.5 s of the same step before and after (untimed):
+    # the timed region alone is ~10 ms, shorter than the sampling interval
+    def load_pad(fn, seconds=0.5):
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < seconds:
+            for _ in range(20):
+                fn()
+            torch.cuda.synchronize()
+
+    clk = ClockSampler(local).__enter__()
+    load_pad(lambda: op32.apply_block(s32["out"]))
     direct = timed(lambda: op32.apply_block(s32["out"]), args.steps, 0)
     graph = None
     try:
@@ -452,13 +472,17 @@ def run_gato(args):
         graph_error = f"{type(exc).__name__}: {exc}"
         per_step = None
     l0 = _lib.launch_count()
-    with ClockSampler(local) as clk:
+    try:
         if graph is not None:
             times = timed(graph.replay, args.steps, 3)
             launches = per_step * args.steps
         else:
             times = timed(lambda: op32.apply_block(s32["out"]), args.steps, 0)
             launches = (_lib.launch_count() - l0) // max(args.steps, 1) * args.steps
+        torch.cuda.synchronize()
+        load_pad(graph.replay if graph is not None else (lambda: op32.apply_block(s32["out"])))
+    finally:
+        clk.__exit__(None, None, None)
     value, t_max = job_rate(sum(times), args.steps, world, dist, dev)
 
     # two steps in flight: the second operator's step replays on its own stream beside the first's
@@ -586,7 +610,8 @@ def run_gato(args):
         "config": {"workload": workload_name(N, h), "precision": "mixed", "N": N, "h": h,
                    "n_occ": N_OCC, "l2": "flushed between steps (256 MiB write)", "parallelism": "replicas",
                    "autotune": tuned},
-        "clocks": clk.summary(),
+        "clocks": dict(clk.summary(), window="the timed direct and graph steps, bracketed by 0.5 s of the same "
+                                              "step before and after"),
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": host_in.numel() * 4,
                 "d2h_bytes_per_step": host_out.numel() * 4,
                 "mode": "two-deep pipeline: step k+1's orbitals copy in and step k-1's result copies out "
@@ -601,12 +626,14 @@ def run_gato(args):
                         "two_streams": two_streams} if graph is not None
                        else {"used": False, "error": graph_error,
                              "direct_launch_value": world * args.steps / sum(direct)}),
-        "roofline": {"kernel": "k_cols<float2, FMI> (x FFT, kernel multiply, inverse x FFT)", "bound": "hbm",
+        "roofline": {"kernel": "packed::k_colsp<16,16,8,FMI> (x FFT, kernel multiply, inverse x FFT; "
+                               "two lines per thread in f32x2)", "bound": "hbm",
                      "achieved": bytes_x / tx_avg / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": bytes_x / tx_avg / 1e9 / peak,
-                     "traffic": FMI_TRAFFIC_128 if N == 128 else None, "peak_kind": peak_kind,
+                     "traffic": FMI_TRAFFIC_128 if N == 128 else None,
+                     "traffic_source": FMI_TRAFFIC_SOURCE if N == 128 else None, "peak_kind": peak_kind,
                      "algorithmic_bytes": bytes_x, "avg_launch_us": tx_avg * 1e6,
-                     "limiter": "instruction issue (75% issue active, FMA pipe 56%, ncu)"},
+                     "limiter": FMI_LIMITER},
         "roofline_stencil": {"bound": "hbm", "achieved": bytes_s / ts_avg / 1e9, "peak": peak, "unit": "GB/s",
                              "frac": bytes_s / ts_avg / 1e9 / peak, "avg_launch_us": ts_avg * 1e6,
                              "timing": "average of back-to-back launches over 4 rotating input sets (302 MB)",

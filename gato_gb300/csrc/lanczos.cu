@@ -1311,47 +1311,41 @@ __global__ void __maxnreg__(96)
   }
 }
 
-// alpha_j and c_j from the sweep's partials (one block): a_k, d_k = dV * sums;
-// b_k = <v_k, v_{j-1}> from the previous sweep (k < j) and d_{j-1} (k = j);
-// alpha_j = a_j - beta_{j-1} b_j; c_k = a_k - beta_{j-1} b_k - alpha_j d_k.
-// Cm row j = c_j; dprev <- d.
-__global__ void k_fz_post1(const double* part, int G, int j, double dV, double* alphas, const double* betas,
-                           double* dprev, double* Cm, int m) {
-  __shared__ double sa[kFzMaxM + 1], sd[kFzMaxM + 1];
-  __shared__ double s_alpha;
-  // one warp per (k, dot): lanes read the block partials in parallel, then a fixed-order tree
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int r = warp; r < 2 * (j + 1); r += nw) {
-    double v = 0.0;
-    for (int q = lane; q < G; q += 32) v += part[(int64_t)r * G + q];
-    v = warp_sum(v);
-    if (lane == 0) {
-      if (r <= j) sa[r] = v * dV;
-      else sd[r - (j + 1)] = v * dV;
-    }
-  }
-  __syncthreads();
-  const double beta = j > 0 ? betas[j - 1] : 0.0;
-  if (threadIdx.x == 0) {
-    const double bj = j > 0 ? sd[j - 1] : 0.0;
-    s_alpha = sa[j] - beta * bj;
-    alphas[j] = s_alpha;
-  }
-  __syncthreads();
-  const double al = s_alpha;
-  for (int k = threadIdx.x; k <= j; k += blockDim.x) {
-    const double bk = j == 0 ? 0.0 : (k < j ? dprev[k] : sd[j - 1]);
-    Cm[(int64_t)j * m + k] = sa[k] - beta * bk - al * sd[k];
-  }
-  __syncthreads();   // every dprev read is done
-  for (int k = threadIdx.x; k <= j; k += blockDim.x) dprev[k] = sd[k];
+// The sweep's row sums, one warp per row r < 2 (j + 1): rs[r] = dV * sum_q part[r G + q] (lanes
+// stride the block partials, then a fixed-order tree), so every sum is the same however many
+// blocks the launch has. Rows r <= j hold a_k, rows j + 1 + k hold d_k.
+__global__ void k_fz_rowsum(const double* part, int G, int rows, double dV, double* rs) {
+  const int lane = threadIdx.x & 31;
+  const int r = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (r >= rows) return;
+  double v = 0.0;
+  for (int q = lane; q < G; q += 32) v += part[(int64_t)r * G + q];
+  v = warp_sum(v);
+  if (lane == 0) rs[r] = v * dV;
 }
 
 // w^_j = u_j - beta_{j-1} v_{j-1} - alpha_j v_j (field type products) and its float-float |.|^2 partials.
+// alpha_j = a_j - beta_{j-1} b_j with b_j = d_{j-1} from the previous sweep, formed by every block
+// from the row sums; block 0 also records alpha_j, row j of Cm, c_k = a_k - beta_{j-1} b_k - alpha_j d_k
+// (b_k = <v_k, v_{j-1}> from the previous sweep for k < j, d_{j-1} for k = j), and dprev <- d.
 __global__ void k_fz_form(const float* __restrict__ U, const float* __restrict__ vm1, const float* __restrict__ vj,
-                          float* wh, int64_t n, const double* betas, const double* alphas, int j, double* part) {
+                          float* wh, int64_t n, const double* rs, double* alphas, const double* betas, double* dprev,
+                          double* Cm, int m, int j, double* part) {
   __shared__ double sh[32];
-  const float be = j > 0 ? (float)betas[j - 1] : 0.f, al = (float)alphas[j];
+  const double* sa = rs;
+  const double* sd = rs + (j + 1);
+  const double beta = j > 0 ? betas[j - 1] : 0.0;
+  const double ald = sa[j] - beta * (j > 0 ? sd[j - 1] : 0.0);
+  if (blockIdx.x == 0) {
+    if (threadIdx.x == 0) alphas[j] = ald;
+    // each thread reads dprev[k] before it overwrites the same entry: no other thread touches it
+    for (int k = threadIdx.x; k <= j; k += blockDim.x) {
+      const double bk = j == 0 ? 0.0 : (k < j ? dprev[k] : sd[j - 1]);
+      Cm[(int64_t)j * m + k] = sa[k] - beta * bk - ald * sd[k];
+      dprev[k] = sd[k];
+    }
+  }
+  const float be = (float)beta, al = (float)ald;
   Acc<float> acc;
   const int64_t nv = n / 4;
   const float4* U4 = reinterpret_cast<const float4*>(U);
@@ -1376,44 +1370,53 @@ __global__ void k_fz_form(const float* __restrict__ U, const float* __restrict__
 }
 
 // beta_j = sqrt(dV |w^_j|^2 - |c_j|^2), binv = {beta_j, 1 / beta_j or 0}, and the next sweep's
-// c = c_j and g_i = sum_k T~_{ik} c_k, i <= j + 1 (one block).
-__global__ void k_fz_post2(const double* part, int nb, double dV, const double* Cm, int m, int j,
-                           const double* alphas, double* betas, double* binv, double* c_next, double* g_next) {
+// c = c_j and g_i = sum_k T~_{ik} c_k, i <= j + 1. Every block forms beta_j from the same sums in
+// the same order (so all hold the same bits) and one warp per g_i sums its column of Cm across the
+// lanes; block 0 writes beta_j, binv and c. Launched with kFzPost2Threads threads per block.
+constexpr int kFzPost2Threads = 256;
+__global__ void __launch_bounds__(kFzPost2Threads)
+    k_fz_post2(const double* part, int nb, double dV, const double* Cm, int m, int j, const double* alphas,
+               double* betas, double* binv, double* c_next, double* g_next) {
   __shared__ double sh[32];
   __shared__ double sc[kFzMaxM + 1];
   double v = 0.0;
   for (int i = threadIdx.x; i < nb; i += blockDim.x) v += part[i];
-  const double wn = block_sum(v, sh);   // valid in thread 0
+  const double wn = block_sum(v, sh);
   double c2 = 0.0;
   for (int k = threadIdx.x; k <= j; k += blockDim.x) {
     const double ck = Cm[(int64_t)j * m + k];
     sc[k] = ck;
-    c_next[k] = ck;
     c2 += ck * ck;
   }
-  __syncthreads();
-  const double cn = block_sum(c2, sh);
-  if (threadIdx.x == 0) {
-    const double b2 = wn * dV - cn;
-    const double beta = b2 > 0.0 ? sqrt(b2) : 0.0;
-    betas[j] = beta;
-    binv[0] = beta;
-    binv[1] = beta > 0.0 ? 1.0 / beta : 0.0;
+  const double cn = block_sum(c2, sh);   // its barriers also publish sc
+  const double b2 = wn * dV - cn;
+  const double beta = b2 > 0.0 ? sqrt(b2) : 0.0;
+  if (blockIdx.x == 0) {
+    if (threadIdx.x == 0) {
+      betas[j] = beta;
+      binv[0] = beta;
+      binv[1] = beta > 0.0 ? 1.0 / beta : 0.0;
+    }
+    for (int k = threadIdx.x; k <= j; k += blockDim.x) c_next[k] = sc[k];
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i <= j + 1; i += blockDim.x) {
-    double gi = 0.0;
+  const int lane = threadIdx.x & 31;
+  const int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (i > j + 1) return;
+  double gi = 0.0;
+  for (int k = i + lane; k <= j; k += 32) gi += sc[k] * Cm[(int64_t)k * m + i];
+  gi = warp_sum(gi);
+  if (lane == 0) {
+    // the tridiagonal part of T~ row i: beta_i c_{i+1} + alpha_i c_i + beta_{i-1} c_{i-1}
     if (i + 1 <= j) gi += sc[i + 1] * betas[i];
     if (i <= j) gi += sc[i] * alphas[i];
-    if (i >= 1) gi += sc[i - 1] * betas[i - 1];
-    for (int k = i; k <= j; ++k) gi += sc[k] * Cm[(int64_t)k * m + i];
+    if (i >= 1) gi += sc[i - 1] * (i - 1 == j ? beta : betas[i - 1]);
     g_next[i] = gi;
   }
 }
 
 struct FzScratch {
   float *wh, *z, *u;
-  double *Cm, *dprev, *c, *g, *binv, *part, *partn;
+  double *Cm, *dprev, *c, *g, *binv, *part, *partn, *rs;
   int grid, nbf, sms;   // grid: the most sweep blocks of any step
 };
 
@@ -1425,7 +1428,8 @@ int fz_scratch(cudaStream_t s, int64_t n, int m, FzScratch& f) {
   f.grid = (int)std::min<int64_t>(n / 64, 4 * (int64_t)sms);
   f.nbf = (int)std::min<int64_t>((n / 4 + 255) / 256, 4 * sms);
   const size_t vec = (size_t)n * sizeof(float);
-  const size_t dbl = (size_t)m * m + m + (m + 1) + (m + 2) + 2 + (size_t)2 * (m + 1) * f.grid + f.nbf;
+  const size_t dbl = (size_t)m * m + m + (m + 1) + (m + 2) + 2 + (size_t)2 * (m + 1) * f.grid + f.nbf +
+                     (size_t)2 * (m + 1);
   unsigned char* p = (unsigned char*)stream_scratch(s, 3 * vec + dbl * sizeof(double) + 256, kSlotLanczosSweep);
   if (!p) return fail(GATO_ENOMEM, "lanczos: sweep scratch allocation failed");
   f.wh = (float*)p;
@@ -1439,6 +1443,7 @@ int fz_scratch(cudaStream_t s, int64_t n, int m, FzScratch& f) {
   f.binv = f.g + (m + 2);
   f.part = f.binv + 2;
   f.partn = f.part + (size_t)2 * (m + 1) * f.grid;
+  f.rs = f.partn + f.nbf;
   return GATO_OK;
 }
 
@@ -1495,12 +1500,15 @@ int lanczos_fused(gato_operator& op, const void* psi0, int m, int K, double tol,
     k_fz_sweep<<<G, kFzThreads, smj, s>>>(*reinterpret_cast<const CUtensorMap*>(tm), Vb, n, j, ce, nst, wh, f.z,
                                           f.u, f.c, f.g, f.binv, f.part, device_error_word());
     GATO_LAUNCH_TRY();
-    k_fz_post1<<<1, 512, 0, s>>>(f.part, G, j, dV, alphas, betas, f.dprev, f.Cm, m);
+    const int rows = 2 * (j + 1);   // one warp per row sum, eight per block
+    k_fz_rowsum<<<(rows + 7) / 8, 256, 0, s>>>(f.part, G, rows, dV, f.rs);
     GATO_LAUNCH_TRY();
     k_fz_form<<<f.nbf, 256, 0, s>>>(f.u, j > 0 ? Vb + (int64_t)(j - 1) * n : nullptr, Vb + (int64_t)j * n, f.wh, n,
-                                    betas, alphas, j, f.partn);
+                                    f.rs, alphas, betas, f.dprev, f.Cm, m, j, f.partn);
     GATO_LAUNCH_TRY();
-    k_fz_post2<<<1, 256, 0, s>>>(f.partn, f.nbf, dV, f.Cm, m, j, alphas, betas, f.binv, f.c, f.g);
+    constexpr int gpb = kFzPost2Threads / 32;   // g_i per block
+    k_fz_post2<<<(j + 2 + gpb - 1) / gpb, kFzPost2Threads, 0, s>>>(f.partn, f.nbf, dV, f.Cm, m, j, alphas, betas,
+                                                                    f.binv, f.c, f.g);
     GATO_LAUNCH_TRY();
     if (j + 1 < m) GATO_TRY(op_apply(op, f.wh, f.z, s));
   }
