@@ -13,8 +13,7 @@
 // Set-up: the first call on each device, with that device current, looks up
 // the array's device address with cudaGetSymbolAddress (the host-side name of
 // a __device__ variable is only a stand-in, never a device pointer) and caches
-// it per device. Make that first call before any stream capture. Every later
-// call allocates nothing and takes no lock.
+// it per device. Every later call allocates nothing and takes no lock.
 //
 // Limits and sharing: one partial sum per 2048-element chunk, so n may not
 // exceed kNoAllocChunks * 2048 = 2^27 elements (a 512^3 grid); larger n is

@@ -74,7 +74,7 @@ int gato_dot(int dtype, const void* a, const void* b, int64_t n, double scale,
  * No counterpart in the reference. Its partial sums live in a library-owned
  * static device array (512 KiB per GPU, resident until exit) instead of
  * lazily allocated scratch; the first call on a device looks up that array's
- * address, so make it before any stream capture. n is limited to 2^27
+ * address and caches it. n is limited to 2^27
  * elements (GATO_EBADARG beyond). Calls share the array: any two calls whose
  * kernels can run at the same time on the GPU race.                      */
 int gato_dot_noalloc(int dtype, const void* a, const void* b, int64_t n, double scale,
