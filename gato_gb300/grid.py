@@ -36,8 +36,8 @@ class Grid3D:
 
     def axis(self, dtype=torch.float64) -> torch.Tensor:
         dev = _lib.require_cuda()
-        a = -self.L / 2 + (torch.arange(self.N, device=dev, dtype=torch.float64) + 0.5) * self.h
-        return a.to(dtype)
+        a = -self.L / 2 + (torch.arange(self.N, dtype=torch.float64) + 0.5) * self.h   # host, then one copy
+        return a.to(dtype).to(dev)
 
     def coords(self, dtype=torch.float64):
         a = self.axis(dtype)
@@ -48,15 +48,28 @@ class Grid3D:
         return torch.sqrt(X * X + Y * Y + Z * Z + softening * softening)
 
 
+_CONVERTIBLE = (torch.float32, torch.float64)
+
+
 def as_field(x, dtype=None) -> torch.Tensor:
-    """A contiguous CUDA tensor view/copy of x (numpy, CPU or CUDA tensor)."""
+    """A contiguous CUDA tensor view/copy of x (numpy, CPU or CUDA tensor).
+
+    Host data is converted and made contiguous on the host and copied once; a contiguous device field
+    changes between FP32 and FP64 through the library's conversion kernel."""
     dev = _lib.require_cuda()
     if not isinstance(x, torch.Tensor):
         x = torch.as_tensor(x)
-    if dtype is not None and x.dtype != dtype:
-        x = x.to(dtype)
     if x.device != dev:
-        x = x.to(dev)
+        if dtype is not None and x.dtype != dtype:
+            x = x.to(dtype)
+        return x.contiguous().to(dev)
+    if dtype is not None and x.dtype != dtype:
+        if x.is_contiguous() and x.numel() > 0 and x.dtype in _CONVERTIBLE and dtype in _CONVERTIBLE:
+            out = torch.empty(x.shape, dtype=dtype, device=dev)
+            _lib.call("gato_convert", _lib.dtype_code(x), C.c_void_p(x.data_ptr()), _lib.dtype_code(out),
+                      C.c_void_p(out.data_ptr()), x.numel(), C.c_void_p(_lib.stream()))
+            return out
+        x = x.to(dtype)
     return x.contiguous()
 
 

@@ -10,6 +10,7 @@ V_H and the energy in FP64; ``"fp64"`` is the plain path.
 from __future__ import annotations
 
 import ctypes as C
+import math
 from dataclasses import dataclass, field
 from typing import Callable
 
@@ -288,10 +289,12 @@ def rhf_energy(orbitals, V_ext, grid: Grid3D, boundary: str = "dirichlet", order
 
 def default_initial_guess(grid: Grid3D, dtype=torch.float64) -> torch.Tensor:
     """(e^{-4r} + e^{-r}) (1 + 0.1(x+y+z) + 0.02(xy+yz+xz)) (scf.py:310-320)."""
-    X, Y, Z = grid.coords()
+    # evaluated on the host in FP64 and copied once (the device runs only the library's kernels)
+    a = -grid.L / 2 + (torch.arange(grid.N, dtype=torch.float64) + 0.5) * grid.h
+    X, Y, Z = torch.meshgrid(a, a, a, indexing="ij")
     r = torch.sqrt(X * X + Y * Y + Z * Z + 1e-6)
     psi0 = (torch.exp(-4.0 * r) + torch.exp(-r)) * (1.0 + 0.1 * (X + Y + Z) + 0.02 * (X * Y + Y * Z + X * Z))
-    return psi0.to(dtype).contiguous()
+    return as_field(psi0, dtype)
 
 
 def _default_initial_orbitals(V_ext, grid: Grid3D, n_occ: int, boundary: str, order: int,
@@ -312,6 +315,11 @@ class SCFResult:
     converged: bool
     energy_history: list = field(default_factory=list)
     terms: torch.Tensor | None = None  # last (kinetic, v_ext, v_nl, hartree, exchange)
+
+
+def _total(terms: torch.Tensor) -> float:
+    """Sum of the five energy terms, read back and added on the host (exactly rounded)."""
+    return math.fsum(terms.tolist())
 
 
 def scf_rhf(V_ext, grid: Grid3D, n_occ: int, *, initial_orbitals=None, max_iters: int = 50,
@@ -384,7 +392,7 @@ def scf_rhf(V_ext, grid: Grid3D, n_occ: int, *, initial_orbitals=None, max_iters
     # throughout.
     energy64 = not mixed
     switch = max(1e3 * tol, 1e-4)
-    orbital_energies = torch.zeros(n_occ, dtype=f64, device=dev)
+    orbital_energies = torch.zeros(n_occ, dtype=f64).to(dev)   # a copy, no device kernel
     converged = False
     terms = None
     it = 0
@@ -411,15 +419,15 @@ def scf_rhf(V_ext, grid: Grid3D, n_occ: int, *, initial_orbitals=None, max_iters
         _lib.call("gato_mix", _lib.F64, P(rho), P(rho_new), n3, float(mixing), s())
         if energy64:
             terms = _energy_terms(orb64, V_ext64, grid, boundary, order, eps, V_nl_apply, op=op64)
-            E = float(terms.sum())
+            E = _total(terms)
         else:
             terms = _energy_terms(orb, V_ext, grid, boundary, order, eps, V_nl_apply, op=op)
-            E = float(terms.sum())
+            E = _total(terms)
             if abs(E - E_prev) < switch:
                 # close to the stop: from here on every energy is FP64, starting with this iterate
                 energy64 = True
                 terms = _energy_terms(orb64, V_ext64, grid, boundary, order, eps, V_nl_apply, op=op64)
-                E = float(terms.sum())
+                E = _total(terms)
                 history.append(E)
                 E_prev = E
                 continue
@@ -431,7 +439,7 @@ def scf_rhf(V_ext, grid: Grid3D, n_occ: int, *, initial_orbitals=None, max_iters
     if not energy64:
         # max_iters reached on FP32 energies: the reported energy is still an FP64 evaluation
         terms = _energy_terms(orb64, V_ext64, grid, boundary, order, eps, V_nl_apply, op=op64)
-        E = float(terms.sum())
+        E = _total(terms)
     return SCFResult(from_fields(orb), E, orbital_energies, it, converged, history, terms)
 
 

@@ -63,7 +63,7 @@ def lanczos(H, psi0, n_iters: int = 80, n_eigenstates: int = 4, tol: float = 1e-
     alphas = torch.empty(m, dtype=torch.float64, device=dev)
     betas = torch.empty(m, dtype=torch.float64, device=dev)
     evals = torch.empty(K, dtype=torch.float64, device=dev)
-    flag = torch.zeros(1, dtype=torch.int32, device=dev)
+    flag = torch.empty(1, dtype=torch.int32, device=dev)   # always written by the eigensolve
     s = C.c_void_p(_lib.stream())
     op = H._gato_operator(dtype) if hasattr(H, "_gato_operator") else None
     if op is not None:
