@@ -332,6 +332,7 @@ namespace cg = cooperative_groups;
 constexpr int kNlCluster = 8;          // CTAs per vector (the portable cluster size)
 constexpr int kNlClThreads = 512;
 constexpr int kNlClMaxQ = 64;          // projectors of all atoms
+constexpr int kNlQChunk = 8;           // projectors of one atom accumulated per pass over its box
 struct NlAtomRange {
   int q0[kMaxAtoms], nq[kMaxAtoms];
 };
@@ -352,19 +353,35 @@ __global__ void __cluster_dims__(kNlCluster, 1, 1) __launch_bounds__(kNlClThread
   const int start = rank * blockDim.x + threadIdx.x, stride = kNlCluster * blockDim.x;
   const T* ps = psi + (int64_t)b * N * N * N;
   T* o = out + (int64_t)b * N * N * N;
-  for (int q = 0; q < nq; ++q) {
-    const int* bx = boxes + 6 * q_atom[q];
+  // overlaps atom by atom, up to kNlQChunk projectors of one atom per pass over its box: a point's
+  // index and psi value serve every projector of the pass (each projector's sum runs over the
+  // thread's points in the same order as a pass of its own)
+  for (int a = 0; a < K; ++a) {
+    const int nqa = ar.nq[a];
+    const int* bx = boxes + 6 * a;
     const int nz = bx[5], nyz = bx[4] * bx[5], npts = bx[3] * nyz;
-    const T* pv = vals + q_off[q];
-    Acc<T> acc;
-    for (int t = start; t < npts; t += stride) {
-      const int x = bx[0] + t / nyz, y = bx[1] + (t % nyz) / nz, z = bx[2] + t % nz;
-      acc.add_prod(pv[t], ps[((int64_t)x * N + y) * N + z]);
-    }
-    double v = acc.value();
+    for (int c0 = 0; c0 < nqa; c0 += kNlQChunk) {
+      const int q0 = ar.q0[a] + c0, nc = min(kNlQChunk, nqa - c0);
+      const T* pv[kNlQChunk];
+      Acc<T> acc[kNlQChunk];
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    if (lane == 0) wsum[q][warp] = v;
+      for (int k = 0; k < kNlQChunk; ++k) pv[k] = vals + q_off[q0 + (k < nc ? k : 0)];
+      for (int t = start; t < npts; t += stride) {
+        const int x = bx[0] + t / nyz, y = bx[1] + (t % nyz) / nz, z = bx[2] + t % nz;
+        const T pst = ps[((int64_t)x * N + y) * N + z];
+#pragma unroll
+        for (int k = 0; k < kNlQChunk; ++k)
+          if (k < nc) acc[k].add_prod(pv[k][t], pst);
+      }
+#pragma unroll
+      for (int k = 0; k < kNlQChunk; ++k) {
+        if (k >= nc) break;
+        double v = acc[k].value();
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) wsum[q0 + k][warp] = v;
+      }
+    }
   }
   __syncthreads();
   if (threadIdx.x < nq) {

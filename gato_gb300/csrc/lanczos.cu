@@ -700,7 +700,10 @@ __device__ __forceinline__ void gershgorin(const double* a, const double* e, int
 // interchanges and reciprocal pivots kept in work) and the factors are applied
 // to the iterate four times (dgtts2). One eigenvalue per block spreads the FP64
 // work over K SMs: GB300's FP64 pipe is narrow, and a Sturm count is a chain
-// of m dependent FP64 divisions. work + k*7m: d, du, du2, f, sw, rd, x.
+// of m dependent FP64 divisions. The factorisation and the iterate live in shared memory (each
+// step of these sequential loops reads what the previous one wrote: in global memory every step
+// would wait on a round trip through L2); the final vector goes to work + k*7m + 6m. Dynamic
+// shared memory: a, e, e2 and d, du, du2, f, sw, rd, x, 10 m doubles.
 __global__ void __launch_bounds__(32) k_tridiag_eig(const double* alpha, const double* beta, int m, int K,
                                                      double* lam_out, double* work, int* err) {
   extern __shared__ double sm[];
@@ -738,7 +741,7 @@ __global__ void __launch_bounds__(32) k_tridiag_eig(const double* alpha, const d
   if (lane != 0) return;
   const double shift = 0.5 * (lo + hi);
   lam_out[k] = shift;
-  double* d = work + (int64_t)k * 7 * m;
+  double* d = e2 + m;
   double* du = d + m;
   double* du2 = du + m;
   double* f = du2 + m;     // multiplier of step i
@@ -798,6 +801,8 @@ __global__ void __launch_bounds__(32) k_tridiag_eig(const double* alpha, const d
     const double inv = 1.0 / nrm;
     for (int i = 0; i < m; ++i) x[i] *= inv;
   }
+  double* xo = work + (int64_t)k * 7 * m + 6 * m;   // read by k_tridiag_finish
+  for (int i = 0; i < m; ++i) xo[i] = x[i];
 }
 
 // Convergence flag (any beta_j < tol for j < max(m-1, 1), lanczos.py:199),
@@ -1048,7 +1053,9 @@ template <typename T>
 int lz_finish(const T* Vb, int64_t n, int m, int K, double tol, const double* alphas,
               const double* betas, double* evals, T* evecs, int* flag, const LzScratch& z,
               cudaStream_t s) {
-  const size_t sme = (size_t)3 * m * sizeof(double);
+  const size_t sme = (size_t)10 * m * sizeof(double);
+  if (sme > 227 * 1024)
+    return fail(GATO_EUNSUPPORTED, "lanczos: m = %d exceeds the tridiagonal eigensolver's shared memory", m);
   if (sme > 48 * 1024)
     GATO_TRY(raise_smem_limit(reinterpret_cast<const void*>(k_tridiag_eig), sme));
   k_tridiag_eig<<<K, 32, sme, s>>>(alphas, betas, m, K, evals, z.work, device_error_word());
