@@ -1318,38 +1318,43 @@ __global__ void __maxnreg__(96)
   }
 }
 
-// The sweep's row sums, one warp per row r < 2 (j + 1): rs[r] = dV * sum_q part[r G + q] (lanes
-// stride the block partials, then a fixed-order tree), so every sum is the same however many
-// blocks the launch has. Rows r <= j hold a_k, rows j + 1 + k hold d_k.
-__global__ void k_fz_rowsum(const double* part, int G, int rows, double dV, double* rs) {
-  const int lane = threadIdx.x & 31;
-  const int r = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  if (r >= rows) return;
-  double v = 0.0;
-  for (int q = lane; q < G; q += 32) v += part[(int64_t)r * G + q];
-  v = warp_sum(v);
-  if (lane == 0) rs[r] = v * dV;
-}
-
-// w^_j = u_j - beta_{j-1} v_{j-1} - alpha_j v_j (field type products) and its float-float |.|^2 partials.
-// alpha_j = a_j - beta_{j-1} b_j with b_j = d_{j-1} from the previous sweep, formed by every block
-// from the row sums; block 0 also records alpha_j, row j of Cm, c_k = a_k - beta_{j-1} b_k - alpha_j d_k
-// (b_k = <v_k, v_{j-1}> from the previous sweep for k < j, d_{j-1} for k = j), and dprev <- d.
+// w^_j = u_j - beta_{j-1} v_{j-1} - alpha_j v_j (field type products) and its float-float |.|^2 partials,
+// with the sweep's projections reduced on the way in. part holds the sweep's block partials, rows
+// r <= j for a_k = dV <v_k, u_j> and rows j + 1 + k for d_k = dV <v_k, v_j>; a row sum is one warp
+// (lanes stride the G partials, then a fixed-order tree), the same sum wherever it runs. Every block
+// forms alpha_j = a_j - beta_{j-1} b_j (b_j = d_{j-1}); warps spread over the blocks form row j of Cm,
+// c_k = a_k - beta_{j-1} b_k - alpha_j d_k (b_k = <v_k, v_{j-1}> from the previous sweep for k < j,
+// d_{j-1} for k = j), and dprev <- d; block 0 records alpha_j.
 __global__ void k_fz_form(const float* __restrict__ U, const float* __restrict__ vm1, const float* __restrict__ vj,
-                          float* wh, int64_t n, const double* rs, double* alphas, const double* betas, double* dprev,
-                          double* Cm, int m, int j, double* part) {
+                          float* wh, int64_t n, const double* part, int G, double dV, double* alphas,
+                          const double* betas, double* dprev, double* Cm, int m, int j, double* partn) {
   __shared__ double sh[32];
-  const double* sa = rs;
-  const double* sd = rs + (j + 1);
+  __shared__ double s_ad[2];   // a_j, d_{j-1}
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  auto rowsum = [&](int r) {
+    double v = 0.0;
+    for (int q = lane; q < G; q += 32) v += part[(int64_t)r * G + q];
+    return warp_sum(v) * dV;
+  };
+  if (warp == 0) {
+    const double aj = rowsum(j);
+    const double dj1 = j > 0 ? rowsum(2 * j) : 0.0;
+    if (lane == 0) {
+      s_ad[0] = aj;
+      s_ad[1] = dj1;
+    }
+  }
+  __syncthreads();
   const double beta = j > 0 ? betas[j - 1] : 0.0;
-  const double ald = sa[j] - beta * (j > 0 ? sd[j - 1] : 0.0);
-  if (blockIdx.x == 0) {
-    if (threadIdx.x == 0) alphas[j] = ald;
-    // each thread reads dprev[k] before it overwrites the same entry: no other thread touches it
-    for (int k = threadIdx.x; k <= j; k += blockDim.x) {
-      const double bk = j == 0 ? 0.0 : (k < j ? dprev[k] : sd[j - 1]);
-      Cm[(int64_t)j * m + k] = sa[k] - beta * bk - ald * sd[k];
-      dprev[k] = sd[k];
+  const double ald = s_ad[0] - beta * s_ad[1];
+  if (blockIdx.x == 0 && threadIdx.x == 0) alphas[j] = ald;
+  for (int k = blockIdx.x * nw + warp; k <= j; k += gridDim.x * nw) {
+    const double sak = rowsum(k), sdk = rowsum(j + 1 + k);
+    if (lane == 0) {
+      // the lane reads dprev[k] before it overwrites the same entry: no other thread touches it
+      const double bk = j == 0 ? 0.0 : (k < j ? dprev[k] : s_ad[1]);
+      Cm[(int64_t)j * m + k] = sak - beta * bk - ald * sdk;
+      dprev[k] = sdk;
     }
   }
   const float be = (float)beta, al = (float)ald;
@@ -1373,7 +1378,7 @@ __global__ void k_fz_form(const float* __restrict__ U, const float* __restrict__
     acc.add_prod(w.w, w.w);
   }
   const double v = block_sum(acc.value(), sh);
-  if (threadIdx.x == 0) part[blockIdx.x] = v;
+  if (threadIdx.x == 0) partn[blockIdx.x] = v;
 }
 
 // beta_j = sqrt(dV |w^_j|^2 - |c_j|^2), binv = {beta_j, 1 / beta_j or 0}, and the next sweep's
@@ -1423,7 +1428,7 @@ __global__ void __launch_bounds__(kFzPost2Threads)
 
 struct FzScratch {
   float *wh, *z, *u;
-  double *Cm, *dprev, *c, *g, *binv, *part, *partn, *rs;
+  double *Cm, *dprev, *c, *g, *binv, *part, *partn;
   int grid, nbf, sms;   // grid: the most sweep blocks of any step
 };
 
@@ -1435,8 +1440,7 @@ int fz_scratch(cudaStream_t s, int64_t n, int m, FzScratch& f) {
   f.grid = (int)std::min<int64_t>(n / 64, 4 * (int64_t)sms);
   f.nbf = (int)std::min<int64_t>((n / 4 + 255) / 256, 4 * sms);
   const size_t vec = (size_t)n * sizeof(float);
-  const size_t dbl = (size_t)m * m + m + (m + 1) + (m + 2) + 2 + (size_t)2 * (m + 1) * f.grid + f.nbf +
-                     (size_t)2 * (m + 1);
+  const size_t dbl = (size_t)m * m + m + (m + 1) + (m + 2) + 2 + (size_t)2 * (m + 1) * f.grid + f.nbf;
   unsigned char* p = (unsigned char*)stream_scratch(s, 3 * vec + dbl * sizeof(double) + 256, kSlotLanczosSweep);
   if (!p) return fail(GATO_ENOMEM, "lanczos: sweep scratch allocation failed");
   f.wh = (float*)p;
@@ -1450,7 +1454,6 @@ int fz_scratch(cudaStream_t s, int64_t n, int m, FzScratch& f) {
   f.binv = f.g + (m + 2);
   f.part = f.binv + 2;
   f.partn = f.part + (size_t)2 * (m + 1) * f.grid;
-  f.rs = f.partn + f.nbf;
   return GATO_OK;
 }
 
@@ -1467,6 +1470,24 @@ __global__ void k_fz_init(double* g, double* binv) {
   binv[1] = 1.0;
 }
 
+// A stream of the Lanczos run's own, with the two events that fork work onto it and join it back
+// (released on every exit; pending work finishes first).
+struct FzSide {
+  cudaStream_t st = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  int create() {
+    GATO_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    GATO_CUDA_TRY(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    GATO_CUDA_TRY(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+    return GATO_OK;
+  }
+  ~FzSide() {
+    if (join) cudaEventDestroy(join);
+    if (fork) cudaEventDestroy(fork);
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
 int lanczos_fused(gato_operator& op, const void* psi0, int m, int K, double tol, float* Vb, double* evals,
                   float* evecs, double* alphas, double* betas, int* flag, cudaStream_t s) {
   const int64_t n = op_n3(op);
@@ -1481,6 +1502,8 @@ int lanczos_fused(gato_operator& op, const void* psi0, int m, int K, double tol,
   GATO_LAUNCH_TRY();
   GATO_TRY(raise_smem_limit(reinterpret_cast<const void*>(k_fz_sweep), kFzSmemCap));
   if (n > INT32_MAX) return fail(GATO_EUNSUPPORTED, "lanczos: field too large for the sweep's tensor map");
+  FzSide side;
+  GATO_TRY(side.create());
   for (int j = 0; j < m; ++j) {
     const float* wh = j == 0 ? Vb : f.wh;   // v_0 itself (beta = 1, c = g = 0) at the first step
     const int ce = fz_ce(j, n);
@@ -1507,17 +1530,20 @@ int lanczos_fused(gato_operator& op, const void* psi0, int m, int K, double tol,
     k_fz_sweep<<<G, kFzThreads, smj, s>>>(*reinterpret_cast<const CUtensorMap*>(tm), Vb, n, j, ce, nst, wh, f.z,
                                           f.u, f.c, f.g, f.binv, f.part, device_error_word());
     GATO_LAUNCH_TRY();
-    const int rows = 2 * (j + 1);   // one warp per row sum, eight per block
-    k_fz_rowsum<<<(rows + 7) / 8, 256, 0, s>>>(f.part, G, rows, dV, f.rs);
-    GATO_LAUNCH_TRY();
     k_fz_form<<<f.nbf, 256, 0, s>>>(f.u, j > 0 ? Vb + (int64_t)(j - 1) * n : nullptr, Vb + (int64_t)j * n, f.wh, n,
-                                    f.rs, alphas, betas, f.dprev, f.Cm, m, j, f.partn);
+                                    f.part, G, dV, alphas, betas, f.dprev, f.Cm, m, j, f.partn);
     GATO_LAUNCH_TRY();
+    // beta_j and the next sweep's coefficients on the side stream, beside the operator apply to w^_j
+    // (which reads neither); the next sweep, and the eigensolve after the last step, wait for them
+    GATO_CUDA_TRY(cudaEventRecord(side.fork, s));
+    GATO_CUDA_TRY(cudaStreamWaitEvent(side.st, side.fork, 0));
     constexpr int gpb = kFzPost2Threads / 32;   // g_i per block
-    k_fz_post2<<<(j + 2 + gpb - 1) / gpb, kFzPost2Threads, 0, s>>>(f.partn, f.nbf, dV, f.Cm, m, j, alphas, betas,
-                                                                    f.binv, f.c, f.g);
+    k_fz_post2<<<(j + 2 + gpb - 1) / gpb, kFzPost2Threads, 0, side.st>>>(f.partn, f.nbf, dV, f.Cm, m, j, alphas,
+                                                                          betas, f.binv, f.c, f.g);
     GATO_LAUNCH_TRY();
+    GATO_CUDA_TRY(cudaEventRecord(side.join, side.st));
     if (j + 1 < m) GATO_TRY(op_apply(op, f.wh, f.z, s));
+    GATO_CUDA_TRY(cudaStreamWaitEvent(s, side.join, 0));
   }
   return lz_finish<float>(Vb, n, m, K, tol, alphas, betas, evals, evecs, flag, z, s);
 }
