@@ -114,3 +114,20 @@ def test_threads_on_packed_shapes_are_bitwise_stable():
     torch.cuda.synchronize()
     assert not errors, errors
     assert not mismatches, mismatches[:8]
+
+
+def test_batch_mixed_64_128_concurrent_equals_sequential():
+    """The batch on 64^3 and 128^3 grids (packed column passes, persistent z forward, one-sweep
+    Lanczos with its side stream, cluster projectors): four systems on three streams give the same
+    energies and forces bit for bit as on one stream, and every energy and force is finite."""
+    from gato_gb300.batch import draw_systems, solve_batch
+    specs = draw_systems(4, seed=4, grids=(64, 128))
+    assert sorted(s.N for s in specs) == [64, 64, 128, 128]
+    seq, _ = solve_batch(specs, streams=1, max_iters=12, tol=1e-6)
+    par, _ = solve_batch(specs, streams=3, max_iters=12, tol=1e-6)
+    assert len({r.stream for r in par}) > 1
+    for a, b in zip(seq, par):
+        assert a.spec.name == b.spec.name
+        assert a.point.energy == b.point.energy, a.spec.name
+        assert torch.equal(a.forces, b.forces), a.spec.name
+        assert torch.isfinite(torch.as_tensor(a.point.energy)) and bool(torch.isfinite(a.forces).all())
