@@ -1172,9 +1172,9 @@ __global__ void __maxnreg__(96)
   unsigned char* base = fzs + ((128u - (smem_u32(fzs) & 127u)) & 127u);
   float* buf0 = reinterpret_cast<float*>(base);
   const int BS = fz_bufstride(j, CE), RW = fz_rw(j, CE), TPK = fz_tpk(j);   // NST staging buffers
-  float* cs = buf0 + (size_t)NST * BS;
-  float* gs = cs + (kFzMaxM + 2);
-  float* pa = gs + (kFzMaxM + 2);                // [2][P-1][CE]: the other groups' partial corrections
+  // (c_k, g_k) pairs, rounded once to FP32: one 8-byte shared load per basis row in phase A
+  float2* csg = reinterpret_cast<float2*>(buf0 + (size_t)NST * BS);
+  float* pa = reinterpret_cast<float*>(csg + (kFzMaxM + 2));   // [2][P-1][CE]: the other groups' partial corrections
   uint64_t* full = reinterpret_cast<uint64_t*>(pa + 4 * kFzCE);   // pa holds up to 2 x 3 x 64 floats
   uint64_t* empty = full + kFzMaxStages;
   __shared__ int abort_flag;
@@ -1189,8 +1189,7 @@ __global__ void __maxnreg__(96)
     abort_flag = 0;
     fence_barrier_init();
   }
-  for (int k = threadIdx.x; k < j; k += blockDim.x) cs[k] = (float)c[k];
-  for (int k = threadIdx.x; k <= j; k += blockDim.x) gs[k] = (float)g[k];
+  for (int k = threadIdx.x; k <= j; k += blockDim.x) csg[k] = make_float2(k < j ? (float)c[k] : 0.f, (float)g[k]);
   __syncthreads();
   if (warp == kFzWarps) {   // producer
     if (lane == 0) {
@@ -1224,7 +1223,7 @@ __global__ void __maxnreg__(96)
   const int k0 = (int)((int64_t)j * h / P), k1 = (int)((int64_t)j * (h + 1) / P);
   const int kb = t / TPK, sub = t % TPK;       // phase B: projection row kb, part sub of the chunk
   const float bi = (float)binv[1];
-  const float gj = gs[j];
+  const float gj = csg[j].y;
   double accA = 0.0, accD = 0.0;
   int it = 0;
   bool ok = true;
@@ -1246,17 +1245,20 @@ __global__ void __maxnreg__(96)
     // phase A: corrections of this half of the basis, two accumulator pairs
     float cv0 = 0.f, cu0 = 0.f, cv1 = 0.f, cu1 = 0.f;
     int k = k0;
+#pragma unroll 2
     for (; k + 1 < k1; k += 2) {
       const float x0 = bf[(size_t)k * RW + e], x1 = bf[(size_t)(k + 1) * RW + e];
-      cv0 = fmaf(cs[k], x0, cv0);
-      cu0 = fmaf(gs[k], x0, cu0);
-      cv1 = fmaf(cs[k + 1], x1, cv1);
-      cu1 = fmaf(gs[k + 1], x1, cu1);
+      const float2 a0 = csg[k], a1 = csg[k + 1];
+      cv0 = fmaf(a0.x, x0, cv0);
+      cu0 = fmaf(a0.y, x0, cu0);
+      cv1 = fmaf(a1.x, x1, cv1);
+      cu1 = fmaf(a1.y, x1, cu1);
     }
     if (k < k1) {
       const float x0 = bf[(size_t)k * RW + e];
-      cv0 = fmaf(cs[k], x0, cv0);
-      cu0 = fmaf(gs[k], x0, cu0);
+      const float2 a0 = csg[k];
+      cv0 = fmaf(a0.x, x0, cv0);
+      cu0 = fmaf(a0.y, x0, cu0);
     }
     float cv = cv0 + cv1, cu = cu0 + cu1;
     if (h > 0) {
