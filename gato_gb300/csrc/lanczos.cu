@@ -1245,7 +1245,7 @@ __global__ void __maxnreg__(96)
     // phase A: corrections of this half of the basis, two accumulator pairs
     float cv0 = 0.f, cu0 = 0.f, cv1 = 0.f, cu1 = 0.f;
     int k = k0;
-#pragma unroll 2
+#pragma unroll 4
     for (; k + 1 < k1; k += 2) {
       const float x0 = bf[(size_t)k * RW + e], x1 = bf[(size_t)(k + 1) * RW + e];
       const float2 a0 = csg[k], a1 = csg[k + 1];
