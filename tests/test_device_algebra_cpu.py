@@ -1,4 +1,6 @@
-"""The one-sweep Lanczos recurrence of the FP32 GPU path, restated in FP64 NumPy on the host.
+"""Algebra the device kernels rely on, restated in FP64 NumPy on the host and checked against the oracle.
+
+1. The one-sweep Lanczos recurrence of the FP32 GPU path.
 
 The device path (``gato_gb300/csrc/lanczos.cu``: ``k_fz_sweep``, ``k_fz_form``, ``k_fz_post2``)
 applies the operator to the three-term vector w^_(j-1) *before* its Gram-Schmidt correction and
@@ -13,9 +15,11 @@ recovers F v_j from the Lanczos relation F V = V T~, so each step reads the basi
             g_i = sum_k T~_ik c_k  with  T~ = tridiag(beta, alpha, beta) + the earlier correction rows.
 
 In exact arithmetic this is the reference's Lanczos with full modified Gram-Schmidt
-reorthogonalisation (``solvers/lanczos.py:110-206``). These tests run both in FP64 on a small
+reorthogonalisation (``solvers/lanczos.py:110-206``). The tests run both in FP64 on a small
 oscillator and hold the tridiagonal coefficients and eigenvalues to rounding-level agreement, so
 the algebra of the GPU recurrence is checked apart from its FP32 arithmetic.
+
+2. The spectral (Parseval) form of the FP64 energy pass, against the oracle's Hockney solve.
 """
 import math
 
@@ -117,3 +121,25 @@ def test_one_sweep_ground_state_energy_is_an_upper_bound_that_converges(oscillat
     e_long = _tridiag_eigs(*one_sweep_lanczos(H, psi0, 60)[:2])[0]
     # Rayleigh-Ritz: more Krylov vectors never raise the lowest Ritz value
     assert e_long <= e_short + 1e-12
+
+
+def test_spectral_energy_identity_of_the_fp64_energy_pass():
+    """The FP64 energy pass (``k_cols_fe``) forms a Hartree-type energy from the x-forward spectrum
+    alone: for two real densities a, b packed as F = a + i b on the doubled grid, with the kernel
+    spectrum G^ real and even, sum_k G^_k |F^_k|^2 / M^3 * dV^2 = <a, J[a]> + <b, J[b]> (Parseval for
+    the circular convolution; the a-b cross terms cancel between k and -k). Checked on the host against
+    the oracle's Hockney solve (``poisson.py:47-79``)."""
+    N, h = 12, 0.4
+    g = o.Grid3D(N, N * h)
+    rng = np.random.default_rng(17)
+    a, b = rng.standard_normal(g.shape), rng.standard_normal(g.shape)
+    eps = h / 2
+    dV = g.h ** 3
+    direct = dV * float(np.sum(a * o.hartree_potential(a, g, eps))) + dV * float(np.sum(b * o.hartree_potential(b, g, eps)))
+    M = 2 * N
+    F = np.zeros((M, M, M), dtype=complex)
+    F[:N, :N, :N] = a + 1j * b
+    Gh = np.fft.fftn(o._coulomb_kernel(N, h, eps))
+    assert np.max(np.abs(Gh.imag)) < 1e-9 * np.max(np.abs(Gh.real))   # real and even
+    spectral = float(np.sum(Gh.real * np.abs(np.fft.fftn(F)) ** 2)) / M ** 3 * dV * dV
+    assert abs(spectral - direct) < 1e-12 * abs(direct)
