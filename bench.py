@@ -34,7 +34,7 @@ sys.path.insert(0, ROOT)
 N_DEFAULT, H_DEFAULT, N_OCC = 128, 0.25, 4
 # DRAM read + write of one x-pass launch (5 fields, 128^3) in the one-kernel ncu capture summarised
 # in profiles/x_pass_fmi_h2o128_f32_packed.md (a recorded figure, not measured by this run)
-FMI_TRAFFIC_128 = 366_578_176 + 274_962_176
+FMI_TRAFFIC_128 = 366_514_944 + 274_889_216
 FMI_TRAFFIC_SOURCE = "profiles/x_pass_fmi_h2o128_f32_packed.md (ncu, same kernel and workload; not re-measured here)"
 FMI_LIMITER = ("packed two-line FFT, 3 CTAs/SM by shared memory (~10 warps): FMA pipe 58%, shared-memory "
                "wavefronts ~60%, issue 44% (ncu); HBM 0.57")
