@@ -36,8 +36,8 @@ N_DEFAULT, H_DEFAULT, N_OCC = 128, 0.25, 4
 # in profiles/x_pass_fmi_h2o128_f32_packed.md (a recorded figure, not measured by this run)
 FMI_TRAFFIC_128 = 366_514_944 + 274_889_216
 FMI_TRAFFIC_SOURCE = "profiles/x_pass_fmi_h2o128_f32_packed.md (ncu, same kernel and workload; not re-measured here)"
-FMI_LIMITER = ("packed two-line FFT, 3 CTAs/SM by shared memory (~10 warps): FMA pipe 58%, shared-memory "
-               "wavefronts ~60%, issue 44% (ncu); HBM 0.57")
+FMI_LIMITER = ("latency: packed two-line FFT, 3 CTAs (12 warps) per SM by shared memory; issue 43%, FMA pipe 58%, "
+               "shared-memory wavefronts 62% (ncu); a 4-CTA layout measured no faster")
 METRIC = "H2O 128^3 RHF block Fock-applies/s (mixed FP32/FP64 at |dE|<1uHa) and force time"
 UNIT = "Fock-applies/s"
 
