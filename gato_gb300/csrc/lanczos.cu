@@ -1101,7 +1101,10 @@ int lz_finish(const T* Vb, int64_t n, int m, int K, double tol, const double* al
 // <v_k, F v_j> and <v_k, v_j> over their chunks (FP32 per chunk, FP64 across
 // chunks). Chunk width, ring depth and blocks per SM follow j (fz_ce,
 // fz_stages). Only the FP32 basis takes this path: FP64 products would make
-// the sweep FP64-bound on GB300.
+// the sweep FP64-bound on GB300. After each sweep, k_fz_form sums the block
+// partials (one warp per row), forms alpha_j, the next correction row and w^_j;
+// k_fz_post2 forms beta_j and the next sweep's coefficients on the run's own
+// side stream while the operator is applied to w^_j.
 constexpr int kFzCE = 128;                  // the middle chunk width; n must be a multiple
 constexpr int kFzWarps = 8;                 // consumer warps
 constexpr int kFzThreads = 32 * (kFzWarps + 1);
